@@ -1,0 +1,124 @@
+"""Generates the golden fixtures of tests/golden/ from the reference's own C++.
+
+Run in a checkout that has the reference tree (default /root/reference, or
+TPD_REFERENCE_ROOT): it builds oracle/_ref/libtpdref.so with oracle/build_ref.py
+and records
+  reference_host.npz   camera matrices (view, projection, proj*view, focal) from
+                       PerspectiveCamera + Camera::lookAt + math::mul, the
+                       getHigherMSB table, and GaussianPoint::fromModel records
+                       of the PLY files below
+  ply_*.ply            small seeded 3DGS PLY files (binary and ASCII)
+The tests compare libtpdsplat's host code against these, bit for bit.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from oracle import build_ref  # noqa: E402
+from torpedo_gb300.configs import FAR, FOV, NEAR, UP, fibonacci_sphere  # noqa: E402
+
+
+def ref_lib():
+    lib = C.CDLL(str(build_ref.build(force=True)))
+    F = C.POINTER(C.c_float)
+    lib.ref_camera.argtypes = [F, F, F, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_float, F, F, F, F]
+    lib.ref_mat4_mul.argtypes = [F, F, F]
+    lib.ref_higher_msb.argtypes = [C.c_uint32]
+    lib.ref_higher_msb.restype = C.c_uint32
+    lib.ref_gaussian_point_size.restype = C.c_uint32
+    lib.ref_from_model.argtypes = [C.c_char_p, F, C.c_uint32]
+    lib.ref_from_model.restype = C.c_uint32
+    return lib
+
+
+def fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def camera_cases():
+    cases = []
+    sizes = [(256, 256), (1920, 1080), (800, 800), (640, 480), (1280, 720), (3840, 2160), (64, 64), (17, 33)]
+    for w, h in sizes:
+        cases.append(((0.0, 0.0, -5.0), (0.0, 0.0, 0.0), UP, w, h, FOV, NEAR, FAR))
+    for i, eye in enumerate(fibonacci_sphere(16)):
+        w, h = sizes[i % len(sizes)]
+        cases.append((tuple(float(x) for x in eye), (0.0, 0.0, 0.0), UP, w, h, FOV, NEAR, FAR))
+    # VolumeSplatting demo camera (demo/VolumeSplatting/main.cpp:108), constructor projection
+    cases.append(((-2.0, -1.0, 0.0), (0.0, 0.0, 0.0), (0.0, -1.0, 0.0), 1280, 720, 0.0, 0.01, 100.0))
+    cases.append(((0.3, -0.7, 2.5), (0.1, 0.2, -0.3), (0.0, 0.0, 1.0), 1920, 1080, 45.0, 0.5, 50.0))
+    return cases
+
+
+def write_ply(path: Path, rng, n: int, n_rest: int, binary: bool):
+    names = ["x", "y", "z", "nx", "ny", "nz", "f_dc_0", "f_dc_1", "f_dc_2"] + [f"f_rest_{i}" for i in range(n_rest)]
+    names += ["opacity", "scale_0", "scale_1", "scale_2", "rot_0", "rot_1", "rot_2", "rot_3"]
+    data = rng.normal(0.0, 1.0, size=(n, len(names))).astype(np.float32)
+    data[:, names.index("scale_0"):names.index("scale_2") + 1] -= 4.0
+    hdr = "ply\nformat {} 1.0\nelement vertex {}\n".format("binary_little_endian" if binary else "ascii", n)
+    hdr += "".join(f"property float {nm}\n" for nm in names) + "end_header\n"
+    with open(path, "wb") as f:
+        f.write(hdr.encode())
+        if binary:
+            f.write(data.astype("<f4").tobytes())
+        else:
+            for row in data:
+                f.write((" ".join(repr(float(v)) for v in row) + "\n").encode())
+
+
+def main():
+    lib = ref_lib()
+    assert lib.ref_gaussian_point_size() == 240
+    cams = camera_cases()
+    out = {}
+    meta = np.zeros((len(cams), 14), np.float32)  # eye3 center3 up3 w h fov near far
+    views, projs, pvs, focals = [], [], [], []
+    for i, (eye, ctr, up, w, h, fov, near, far) in enumerate(cams):
+        e, c, u = (np.asarray(v, np.float32) for v in (eye, ctr, up))
+        v = np.zeros(16, np.float32); p = np.zeros(16, np.float32); pv = np.zeros(16, np.float32)
+        fo = np.zeros(2, np.float32)
+        lib.ref_camera(fp(e), fp(c), fp(u), w, h, fov, near, far, fp(v), fp(p), fp(pv), fp(fo))
+        meta[i] = [*eye, *ctr, *up, w, h, fov, near, far]
+        views.append(v); projs.append(p); pvs.append(pv); focals.append(fo)
+    out["cam_meta"] = meta
+    out["cam_view"] = np.stack(views)
+    out["cam_proj"] = np.stack(projs)
+    out["cam_projview"] = np.stack(pvs)
+    out["cam_focal"] = np.stack(focals)
+
+    rng = np.random.default_rng(1234)
+    a = rng.normal(0, 3, size=(32, 16)).astype(np.float32)
+    b = rng.normal(0, 3, size=(32, 16)).astype(np.float32)
+    prod = np.zeros((32, 16), np.float32)
+    for i in range(32):
+        r = np.zeros(16, np.float32)
+        lib.ref_mat4_mul(fp(np.ascontiguousarray(a[i])), fp(np.ascontiguousarray(b[i])), fp(r))
+        prod[i] = r
+    out["mul_a"], out["mul_b"], out["mul_ab"] = a, b, prod
+
+    tiles = sorted(set([0, 1, 2, 3, 255, 256, 257, 1200, 2500, 3600, 8160, 8192, 32400, 65535, 65536, 65537,
+                        1 << 20, (1 << 31) + 5] + [int(x) for x in rng.integers(1, 1 << 24, size=64)]))
+    out["msb_n"] = np.asarray(tiles, np.uint32)
+    out["msb_ref"] = np.asarray([lib.ref_higher_msb(t) for t in tiles], np.uint32)
+
+    for name, n, n_rest, binary in [("ply_deg3_binary", 96, 45, True), ("ply_deg1_ascii", 24, 9, False)]:
+        path = HERE / f"{name}.ply"
+        write_ply(path, rng, n, n_rest, binary)
+        cnt = lib.ref_from_model(str(path).encode(), None, 0)
+        rec = np.zeros((cnt, 60), np.float32)
+        lib.ref_from_model(str(path).encode(), fp(rec), cnt)
+        out[f"{name}_records"] = rec
+
+    np.savez_compressed(HERE / "reference_host.npz", **out)
+    print("wrote", HERE / "reference_host.npz", {k: v.shape for k, v in out.items()})
+
+
+if __name__ == "__main__":
+    main()

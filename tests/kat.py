@@ -1,0 +1,92 @@
+"""Hand-built known-answer scenes shared by the oracle and GPU tests.
+
+Each builder returns (records, camera) with expected values worked out by hand
+from the shaders' formulas (project.slang, splat/*.slang, blend.slang)."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+import torpedo_gb300 as T
+
+C0 = 0.28209479177387814
+
+
+def rgb2sh(r, g, b):
+    sh = np.zeros(48, np.float32)
+    sh[0], sh[1], sh[2] = (r - 0.5) / C0, (g - 0.5) / C0, (b - 0.5) / C0
+    return sh
+
+
+def record(pos, opacity, scale, quat=(0, 0, 0, 1), sh=None, modifier=1.0):
+    r = np.zeros(60, np.float32)
+    r[0:3] = pos
+    r[3] = opacity
+    r[4:8] = quat
+    r[8:11] = scale
+    r[11] = modifier
+    r[12:60] = rgb2sh(0.5, 0.5, 0.5) if sh is None else sh
+    return r
+
+
+def camera(w=256, h=256):
+    return T.Camera.orbit((0.0, 0.0, -5.0), w, h)
+
+
+def single_isotropic():
+    """One isotropic Gaussian at the origin, seen from (0,0,-5): centred at pixel (127.5, 127.5)."""
+    cam = camera()
+    rec = record((0, 0, 0), 0.8, (0.05, 0.05, 0.05), sh=rgb2sh(0.2, 0.4, 0.6))[None]
+    fy = float(cam.proj[1, 1])
+    focal = 0.5 * 256 * fy
+    var = (focal / 5.0) ** 2 * 0.05 ** 2 + 0.3
+    # isotropic: mid^2 - det = 0, so the shader's max(0.1, .) adds sqrt(0.1) to the eigenvalue
+    lam = var + math.sqrt(0.1)
+    exp = dict(px=127.5, py=127.5, depth=5.0, conic=(1 / var, 0.0, 1 / var), radius=math.ceil(3 * math.sqrt(lam)),
+               color=(0.2, 0.4, 0.6), var=var,
+               # with the band-3 quirk (common.slang:69) the scalar C3[3]*z*(2zz-3xx-3yy) is added to
+               # every channel; on the optical axis dir = (0, 0, 1) it is 2*C3[3]
+               compat_shift=2 * 0.3731763325901154)
+    x0 = int((127.5 - exp["radius"]) / 16)
+    x1 = int((127.5 + exp["radius"] + 15) / 16)
+    exp["tiles"] = (x1 - x0) * (x1 - x0)
+    return rec, cam, exp
+
+
+def two_depths():
+    """Red in front (depth 4), blue behind (depth 6), both centred."""
+    cam = camera()
+    recs = np.stack([record((0, 0, 1.0), 0.5, (0.08,) * 3, sh=rgb2sh(0.0, 1.0, 1.0)),   # depth 6, index 0
+                     record((0, 0, -1.0), 0.6, (0.08,) * 3, sh=rgb2sh(1.0, 0.0, 0.0))])  # depth 4, index 1
+    return recs, cam
+
+
+def culled():
+    """Behind the camera, outside the left/right planes, beyond far: all culled."""
+    cam = camera()
+    recs = np.stack([record((0, 0, -6.0), 0.9, (0.1,) * 3), record((10.0, 0, 0), 0.9, (0.1,) * 3),
+                     record((0, 0, 200.0), 0.9, (0.1,) * 3)])
+    return recs, cam
+
+
+def tile_edge():
+    """Gaussians whose centre lies on tile boundaries and at image corners."""
+    cam = camera()
+    fy = float(cam.proj[1, 1])
+    recs = []
+    for px in (15.5, 16.0, 127.5, 0.0, 255.0):
+        # pixel -> ndc -> world x at depth 5
+        ndc = (2 * px + 1) / 256 - 1
+        x = ndc * 5.0 / fy
+        recs.append(record((x, x * 0.5, 0.0), 0.7, (0.03, 0.02, 0.04)))
+    return np.stack(recs), cam
+
+
+def sh_probe(k: int):
+    """One Gaussian on the axis with a single SH feature k (1..15) set to 1 in channel 0."""
+    cam = camera()
+    sh = np.zeros(48, np.float32)
+    sh[3 + 0 * 15 + (k - 1)] = 1.0
+    rec = record((0.3, -0.2, 0.5), 0.9, (0.05,) * 3, sh=sh)[None]
+    return rec, cam

@@ -1,0 +1,291 @@
+// blend.cu — kernel (e): per-tile front-to-back alpha blending, and its adjoint.
+//
+// Reference: blend.slang:24-105 (one 16x16 workgroup per tile; rounds of 256
+// splats staged in shared memory; per pixel: power, alpha = min(0.99,
+// o*exp(power)), skip below 1/255, stop when T*(1-alpha) < 1e-4; colour
+// gathered per contributing pair) dispatched by GaussianEngine.cpp:857-862.
+// The reference has no backward pass; blend_backward_kernel is new.
+//
+// GB300 form: a CTA of 256 threads per tile; each round stages position,
+// conic+opacity and colour of 256 list entries into shared memory (colour is
+// staged with the rest instead of gathered per pair), the whole CTA leaves as
+// soon as every pixel is done (__syncthreads_count), and per pixel the final
+// transmittance and the number of list entries up to the last contributor
+// are kept for the adjoint. The adjoint walks each tile's list back to front,
+// recomputing transmittance as T / (1 - alpha) from the final T (no per-pixel
+// lists), and accumulates per-Gaussian gradients warp-reduced, then in
+// shared memory, then with one global atomic per (round, Gaussian, field).
+//
+// power/alpha are computed by one inline function with explicit rounding
+// intrinsics, so the forward and the adjoint take identical decisions.
+#include "tpd_common.cuh"
+#include "tpd_kernels.h"
+
+namespace tpd {
+namespace {
+
+constexpr uint32_t kBlendThreads = kTilePixels;  // 256
+constexpr float kAlphaMin = 1.0f / 255.0f;
+constexpr float kAlphaMax = 0.99f;
+constexpr float kTMin = 0.0001f;
+
+struct PairEval {
+    float dx, dy, G, alpha, raw_alpha;
+};
+
+// -0.5 * (cx*dx*dx + cz*dy*dy) - cy*dx*dy with d = xy - pixel (blend.slang:83-84).
+__device__ __forceinline__ float pair_power(float2 xy, float4 co, float pxf, float pyf, float& dx, float& dy) {
+    dx = __fsub_rn(xy.x, pxf);
+    dy = __fsub_rn(xy.y, pyf);
+    const float q = __fmaf_rn(__fmul_rn(co.x, dx), dx, __fmul_rn(__fmul_rn(co.z, dy), dy));
+    return __fmaf_rn(-0.5f, q, -__fmul_rn(__fmul_rn(co.y, dx), dy));
+}
+
+__device__ __forceinline__ void load_view_tile(const BlendArgs* /*unused*/, const ViewConst* views,
+                                               const uint32_t* tile_view, uint32_t tile, uint32_t& vi,
+                                               uint32_t& width, uint32_t& height, uint32_t& tx, uint32_t& ty) {
+    vi = tile_view ? tile_view[tile] : 0u;
+    const ViewConst& v = views[vi];
+    width = v.width;
+    height = v.height;
+    const uint32_t local = tile - v.tile_base;
+    const uint32_t gx = grid_x(width);
+    tx = local % gx;
+    ty = local / gx;
+}
+
+__global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
+    __shared__ float2 s_xy[kBlendThreads];
+    __shared__ float4 s_co[kBlendThreads];
+    __shared__ float4 s_col[kBlendThreads];
+
+    const uint32_t tile = blockIdx.x;
+    if (a.ctl->status & kStatusFatal) return;
+    uint32_t vi, W, H, tx, ty;
+    load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t pxl = tx * kBlockX + (tid % kBlockX), pyl = ty * kBlockY + (tid / kBlockX);
+    const bool inside = pxl < W && pyl < H;
+    const float pxf = float(pxl), pyf = float(pyl);
+    const uint32_t K = min(a.ctl->total_keys, a.capacity);
+    const uint32_t end = min(a.ranges[tile * 2 + 1], K), start = min(a.ranges[tile * 2 + 0], end);
+    const Splat* vsplats = a.splats + size_t(vi) * a.n;
+
+    bool done = !inside;
+    float T = 1.0f, C0 = 0.f, C1 = 0.f, C2 = 0.f;
+    uint32_t last = 0;
+    for (uint32_t b0 = start; b0 < end; b0 += kBlendThreads) {
+        if (__syncthreads_count(done) == kBlendThreads) break;
+        const uint32_t j = b0 + tid;
+        if (j < end) {
+            const uint32_t idx = a.vals[j];
+            if (idx < a.n) {
+                const float4* sp = reinterpret_cast<const float4*>(vsplats + idx);
+                const float4 col = __ldg(sp + 0), tex = __ldg(sp + 1), co = __ldg(sp + 2);
+                s_xy[tid] = make_float2(tex.x, tex.y);
+                s_co[tid] = co;
+                s_col[tid] = col;
+            } else {  // only reachable with corrupted lists: an entry that never contributes
+                s_xy[tid] = make_float2(0.f, 0.f);
+                s_co[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+                s_col[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+        __syncthreads();
+        const uint32_t n = min(kBlendThreads, end - b0);
+        if (!done) {
+            for (uint32_t jj = 0; jj < n; ++jj) {
+                float dx, dy;
+                const float4 co = s_co[jj];
+                const float power = pair_power(s_xy[jj], co, pxf, pyf, dx, dy);
+                if (power > 0.0f) continue;
+                const float alpha = fminf(kAlphaMax, __fmul_rn(co.w, __expf(power)));
+                if (alpha < kAlphaMin) continue;
+                const float tn = __fmul_rn(T, __fsub_rn(1.0f, alpha));
+                if (tn < kTMin) {
+                    done = true;
+                    break;
+                }
+                const float4 col = s_col[jj];
+                const float w = __fmul_rn(alpha, T);
+                C0 = __fmaf_rn(col.x, w, C0);
+                C1 = __fmaf_rn(col.y, w, C1);
+                C2 = __fmaf_rn(col.z, w, C2);
+                T = tn;
+                last = b0 + jj - start + 1;
+            }
+        }
+    }
+    if (inside) {
+        const size_t p = (a.image_offset ? a.image_offset[vi] : 0ull) + size_t(pyl) * W + pxl;
+        a.image[p * 3 + 0] = C0;
+        a.image[p * 3 + 1] = C1;
+        a.image[p * 3 + 2] = C2;
+        if (a.final_T) a.final_T[p] = T;
+        if (a.n_contrib) a.n_contrib[p] = last;
+    }
+}
+
+// UNORM conversion of (r, g, b, 1): round(clamp(c, 0, 1) * 255).
+__global__ void pack_rgba8_kernel(const float* rgb, uint32_t* rgba, size_t pixels) {
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= pixels) return;
+    uint32_t out = 0xFF000000u;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float v = fminf(fmaxf(rgb[i * 3 + c], 0.0f), 1.0f);
+        out |= uint32_t(__float2uint_rn(v * 255.0f)) << (8 * c);
+    }
+    rgba[i] = out;
+}
+
+__device__ __forceinline__ float warp_red(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+constexpr int kG2D = 9;  // px, py, conic.x, conic.y, conic.z, opacity, r, g, b
+
+__global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBackwardArgs a) {
+    __shared__ float2 s_xy[kBlendThreads];
+    __shared__ float4 s_co[kBlendThreads];
+    __shared__ float4 s_col[kBlendThreads];
+    __shared__ uint32_t s_idx[kBlendThreads];
+    __shared__ float s_acc[kBlendThreads][kG2D + 1];
+
+    const uint32_t tile = blockIdx.x;
+    if (a.ctl->status & kStatusFatal) return;
+    uint32_t vi, W, H, tx, ty;
+    load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    const uint32_t pxl = tx * kBlockX + (tid % kBlockX), pyl = ty * kBlockY + (tid / kBlockX);
+    const bool inside = pxl < W && pyl < H;
+    const float pxf = float(pxl), pyf = float(pyl);
+    const uint32_t K = min(a.ctl->total_keys, a.capacity);
+    const uint32_t end = min(a.ranges[tile * 2 + 1], K), start = min(a.ranges[tile * 2 + 0], end);
+    const Splat* vsplats = a.splats + size_t(vi) * a.n;
+
+    const size_t p = (a.image_offset ? a.image_offset[vi] : 0ull) + size_t(pyl) * W + pxl;
+    float T = 1.0f, g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    uint32_t last = 0;
+    if (inside) {
+        T = a.final_T[p];
+        last = min(a.n_contrib[p], end - start);
+        g0 = a.dL_dimage[p * 3 + 0];
+        g1 = a.dL_dimage[p * 3 + 1];
+        g2 = a.dL_dimage[p * 3 + 2];
+    }
+    // the block walks back from the largest last-contributor index over its pixels
+    uint32_t max_last = last;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) max_last = max(max_last, __shfl_xor_sync(0xFFFFFFFFu, max_last, o));
+    __shared__ uint32_t s_max[kBlendThreads / 32];
+    if (lane == 0) s_max[tid >> 5] = max_last;
+    __syncthreads();
+    max_last = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kBlendThreads / 32; ++w) max_last = max(max_last, s_max[w]);
+
+    float S0 = 0.f, S1 = 0.f, S2 = 0.f;  // colour accumulated behind the current entry
+    float* g2d_view = a.g2d + size_t(vi) * a.g2d_view_stride;
+    for (int32_t r_end = int32_t(max_last); r_end > 0; r_end -= int32_t(kBlendThreads)) {
+        const int32_t r0 = max(0, r_end - int32_t(kBlendThreads));
+        const uint32_t n = uint32_t(r_end - r0);
+        __syncthreads();
+        if (tid < n) {
+            const uint32_t e = uint32_t(r_end) - 1u - tid;  // descending list position (relative)
+            uint32_t idx = a.vals[start + e];
+            if (idx < a.n) {
+                const float4* sp = reinterpret_cast<const float4*>(vsplats + idx);
+                const float4 col = __ldg(sp + 0), tex = __ldg(sp + 1), co = __ldg(sp + 2);
+                s_xy[tid] = make_float2(tex.x, tex.y);
+                s_co[tid] = co;
+                s_col[tid] = col;
+            } else {  // only reachable with corrupted lists
+                idx = 0;
+                s_xy[tid] = make_float2(0.f, 0.f);
+                s_co[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+                s_col[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            s_idx[tid] = idx;
+        }
+        for (uint32_t k = tid; k < kBlendThreads * (kG2D + 1); k += kBlendThreads) (&s_acc[0][0])[k] = 0.f;
+        __syncthreads();
+        for (uint32_t jj = 0; jj < n; ++jj) {
+            const uint32_t e = uint32_t(r_end) - 1u - jj;
+            float gv[kG2D];
+#pragma unroll
+            for (int k = 0; k < kG2D; ++k) gv[k] = 0.f;
+            bool contrib = false;
+            if (inside && e < last) {
+                float dx, dy;
+                const float4 co = s_co[jj];
+                const float power = pair_power(s_xy[jj], co, pxf, pyf, dx, dy);
+                if (power <= 0.0f) {
+                    const float G = __expf(power);
+                    const float raw = __fmul_rn(co.w, G);
+                    const float alpha = fminf(kAlphaMax, raw);
+                    if (alpha >= kAlphaMin) {
+                        contrib = true;
+                        const float one_m = 1.0f - alpha;
+                        const float Tb = T / one_m;  // transmittance in front of this entry
+                        const float4 col = s_col[jj];
+                        const float w = alpha * Tb;
+                        gv[6] = g0 * w;
+                        gv[7] = g1 * w;
+                        gv[8] = g2 * w;
+                        const float dA = g0 * (col.x * Tb - S0 / one_m) + g1 * (col.y * Tb - S1 / one_m) +
+                                         g2 * (col.z * Tb - S2 / one_m);
+                        S0 = fmaf(col.x, w, S0);
+                        S1 = fmaf(col.y, w, S1);
+                        S2 = fmaf(col.z, w, S2);
+                        T = Tb;
+                        if (raw <= kAlphaMax) {
+                            const float dpow = dA * alpha;
+                            gv[5] = dA * G;
+                            gv[0] = dpow * (-co.x * dx - co.y * dy);
+                            gv[1] = dpow * (-co.z * dy - co.y * dx);
+                            gv[2] = dpow * (-0.5f * dx * dx);
+                            gv[3] = dpow * (-dx * dy);
+                            gv[4] = dpow * (-0.5f * dy * dy);
+                        }
+                    }
+                }
+            }
+            if (__any_sync(0xFFFFFFFFu, contrib)) {
+#pragma unroll
+                for (int k = 0; k < kG2D; ++k) gv[k] = warp_red(gv[k]);
+                if (lane == 0) {
+#pragma unroll
+                    for (int k = 0; k < kG2D; ++k) atomicAdd(&s_acc[jj][k], gv[k]);
+                }
+            }
+        }
+        __syncthreads();
+        for (uint32_t k = tid; k < n * kG2D; k += kBlendThreads) {
+            const uint32_t jj = k / kG2D, f = k % kG2D;
+            const float v = s_acc[jj][f];
+            if (v != 0.0f) atomicAdd(g2d_view + size_t(s_idx[jj]) * a.g2d_stride + f, v);
+        }
+    }
+}
+
+}  // namespace
+
+void launch_blend(const BlendArgs& a, cudaStream_t s) {
+    if (a.n_tiles == 0) return;
+    blend_kernel<<<a.n_tiles, kBlendThreads, 0, s>>>(a);
+}
+
+void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStream_t s) {
+    if (pixels == 0) return;
+    pack_rgba8_kernel<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(rgb, rgba, pixels);
+}
+
+void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s) {
+    if (a.n_tiles == 0) return;
+    blend_backward_kernel<<<a.n_tiles, kBlendThreads, 0, s>>>(a);
+}
+
+}  // namespace tpd

@@ -1,0 +1,839 @@
+// engine.cu — the C ABI (include/tpdsplat.h): engine state, buffers and the
+// per-frame schedule.
+//
+// Reference: GaussianEngine (volumetric/src/GaussianEngine.cpp). Differences
+// by design:
+//  - The reference reads tilesRendered back to the host in the middle of every
+//    frame (GaussianEngine.cpp:665-674) to size its key buffers. Here every
+//    kernel after the scan reads K from device memory and the key buffers have
+//    a capacity: keygen drops keys past it and raises a status bit, and the
+//    host grows the buffers and re-runs the frame. A frame therefore has no
+//    host round trip and is replayed as one CUDA graph.
+//  - One stream, no queue-ownership transfers; images stay in device memory
+//    until tpd_read_image (the reference copies into a swapchain image).
+//  - Host waits poll an event with a time limit (the reference waits on
+//    fences with UINT64_MAX, GaussianEngine.cpp:634, 665).
+//  - V >= 1 views per frame; V = 1 reproduces the reference's keys exactly
+//    (tile ids without offset).
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/tpdsplat.h"
+#include "tpd_common.cuh"
+#include "tpd_kernels.h"
+
+using namespace tpd;
+
+namespace {
+
+constexpr uint32_t kDefaultSpin = 1u << 20;
+constexpr uint32_t kPreThreads = 128;
+constexpr uint32_t kScanTileStandalone = 1024;
+
+struct StatsHead {
+    uint32_t status, tag, total_keys, visible;
+};
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+}  // namespace
+
+struct tpd_engine {
+    tpd_settings settings{};
+    int device = 0;
+    int num_sms = 148;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string last_error;
+    cudaEvent_t done_event = nullptr;
+
+    // scene
+    uint32_t n = 0;
+    uint32_t n_ent = 1;
+    bool compiled = false;
+    float* d_recs = nullptr;
+    uint32_t* d_ent_idx = nullptr;
+    float* h_transforms = nullptr;  // pinned, n_ent x 16
+    float* d_transforms = nullptr;
+    bool identity_transforms = true;
+
+    // views
+    uint32_t n_views = 0;
+    ViewConst* h_views = nullptr;  // pinned, kMaxViews
+    ViewConst* d_views = nullptr;
+    std::vector<uint32_t> vw, vh;
+    uint32_t total_tiles = 0;
+    uint64_t total_pixels = 0;
+    uint32_t* d_tile_view = nullptr;
+    uint64_t* d_image_offset = nullptr;
+
+    // frame buffers
+    uint64_t splat_cap = 0;  // entries of splats / offsets (views x n)
+    Splat* d_splats = nullptr;
+    uint32_t* d_offsets = nullptr;
+    uint64_t* d_desc_pre = nullptr;
+    uint64_t desc_pre_cap = 0;
+    float* d_ent_mats = nullptr;
+    uint64_t ent_mats_cap = 0;
+    uint64_t capacity = 0;
+    uint64_t* d_keys[2] = {nullptr, nullptr};
+    uint32_t* d_vals[2] = {nullptr, nullptr};
+    uint64_t* d_desc_sort = nullptr;
+    uint32_t* d_ranges = nullptr;
+    uint64_t pixel_cap = 0, tile_cap = 0;
+    float* d_image = nullptr;
+    float* d_final_T = nullptr;
+    uint32_t* d_n_contrib = nullptr;
+    uint32_t* d_rgba = nullptr;
+    float* d_g2d = nullptr;
+    uint64_t g2d_cap = 0;
+    float* d_gscratch = nullptr;
+    uint64_t gscratch_cap = 0;
+    FrameCtl* d_ctl = nullptr;
+    StatsHead* h_stats = nullptr;  // pinned
+
+    uint32_t key_bits = 0, passes = 0;
+    bool sorted_in_alt = false;
+    bool frame_valid = false;
+
+    // stage timing: a ring of event sets, harvested at synchronisation points
+    static constexpr int kTimingSlots = 64;
+    static constexpr int kTimingEvents = TPD_STAGE_COUNT + 1;
+    cudaEvent_t tev[kTimingSlots][kTimingEvents] = {};
+    bool tev_pending[kTimingSlots] = {};
+    int tslot = 0;
+    double stage_ms[TPD_STAGE_COUNT] = {};
+    uint64_t timed_frames = 0;
+
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    bool needs_eager = true;  // the first frame after any change runs without a graph
+    uint64_t frames = 0;
+};
+
+namespace {
+
+int fail(tpd_engine* e, int code, const std::string& msg) {
+    if (e) e->last_error = msg;
+    return code;
+}
+
+#define TPD_CUDA(e, call)                                                                                  \
+    do {                                                                                                   \
+        cudaError_t _err = (call);                                                                         \
+        if (_err != cudaSuccess) {                                                                         \
+            return fail((e), _err == cudaErrorMemoryAllocation ? TPD_ERR_OOM : TPD_ERR_DEVICE,             \
+                        std::string(#call) + ": " + cudaGetErrorString(_err));                             \
+        }                                                                                                  \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T*& p, uint64_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+}
+
+void invalidate_graph(tpd_engine* e) {
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+    e->graph_valid = false;
+    e->needs_eager = true;
+}
+
+// Views x n sized buffers.
+int ensure_splat_buffers(tpd_engine* e) {
+    const uint64_t need = uint64_t(e->n) * e->n_views;
+    if (need > e->splat_cap) {
+        invalidate_graph(e);
+        TPD_CUDA(e, dalloc(e->d_splats, need));
+        TPD_CUDA(e, dalloc(e->d_offsets, need));
+        e->splat_cap = need;
+    }
+    const uint64_t parts = (uint64_t(e->n) + kPreThreads - 1) / kPreThreads + 1;
+    if (parts > e->desc_pre_cap) {
+        invalidate_graph(e);
+        TPD_CUDA(e, dalloc(e->d_desc_pre, parts));
+        TPD_CUDA(e, cudaMemset(e->d_desc_pre, 0, parts * 8));
+        e->desc_pre_cap = parts;
+    }
+    const uint64_t em = uint64_t(e->n_ent) * e->n_views * kEntityMatFloats;
+    if (em > e->ent_mats_cap) {
+        invalidate_graph(e);
+        TPD_CUDA(e, dalloc(e->d_ent_mats, em));
+        e->ent_mats_cap = em;
+    }
+    return TPD_OK;
+}
+
+int ensure_key_capacity(tpd_engine* e, uint64_t want) {
+    if (want <= e->capacity) return TPD_OK;
+    if (want > 0x7FFFFFFFull) return fail(e, TPD_ERR_CAPACITY, "key count exceeds 2^31-1");
+    invalidate_graph(e);
+    for (int b = 0; b < 2; ++b) {
+        TPD_CUDA(e, dalloc(e->d_keys[b], want));
+        TPD_CUDA(e, dalloc(e->d_vals[b], want));
+    }
+    const size_t entries = sort_desc_entries(uint32_t(want));
+    TPD_CUDA(e, dalloc(e->d_desc_sort, entries));
+    TPD_CUDA(e, cudaMemset(e->d_desc_sort, 0, entries * 8));
+    e->capacity = want;
+    return TPD_OK;
+}
+
+int wait_stream(tpd_engine* e) {
+    TPD_CUDA(e, cudaEventRecord(e->done_event, e->stream));
+    const double limit = e->settings.timeout_s > 0 ? e->settings.timeout_s : 60.0;
+    const auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        const cudaError_t q = cudaEventQuery(e->done_event);
+        if (q == cudaSuccess) return TPD_OK;
+        if (q != cudaErrorNotReady) return fail(e, TPD_ERR_DEVICE, std::string("frame: ") + cudaGetErrorString(q));
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (dt > limit) return fail(e, TPD_ERR_TIMEOUT, "frame did not finish within the host wait limit");
+        std::this_thread::sleep_for(std::chrono::microseconds(dt < 0.01 ? 20 : 500));
+    }
+}
+
+void harvest_slot(tpd_engine* e, int slot) {
+    if (!e->tev_pending[slot]) return;
+    cudaEventSynchronize(e->tev[slot][tpd_engine::kTimingEvents - 1]);
+    for (int k = 0; k < TPD_STAGE_COUNT; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e->tev[slot][k], e->tev[slot][k + 1]) == cudaSuccess) e->stage_ms[k] += ms;
+    }
+    e->timed_frames++;
+    e->tev_pending[slot] = false;
+}
+
+void harvest_all(tpd_engine* e) {
+    for (int i = 0; i < tpd_engine::kTimingSlots; ++i) harvest_slot(e, i);
+}
+
+// Enqueues one frame on the stream (no host synchronisation).
+void enqueue_frame(tpd_engine* e) {
+    cudaStream_t s = e->stream;
+    cudaEvent_t* ev = nullptr;
+    if (e->settings.stage_timing) {
+        const int slot = e->tslot;
+        e->tslot = (e->tslot + 1) % tpd_engine::kTimingSlots;
+        harvest_slot(e, slot);
+        if (!e->tev[slot][0])
+            for (int k = 0; k < tpd_engine::kTimingEvents; ++k) cudaEventCreate(&e->tev[slot][k]);
+        ev = e->tev[slot];
+        e->tev_pending[slot] = true;
+    }
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], s);
+    };
+    mark(0);
+    cudaMemcpyAsync(e->d_views, e->h_views, sizeof(ViewConst) * e->n_views, cudaMemcpyHostToDevice, s);
+    if (!e->identity_transforms)
+        cudaMemcpyAsync(e->d_transforms, e->h_transforms, sizeof(float) * 16 * e->n_ent, cudaMemcpyHostToDevice, s);
+    launch_frame_begin(e->d_ctl, e->identity_transforms ? nullptr : e->d_transforms, e->n_ent, e->d_views,
+                       e->n_views, e->d_ent_mats, s);
+    PreprocessArgs pa{};
+    pa.recs = e->d_recs;
+    pa.n = e->n;
+    pa.ent_idx = e->d_ent_idx;
+    pa.ent_mats = e->d_ent_mats;
+    pa.n_ent = e->n_ent;
+    pa.views = e->d_views;
+    pa.n_views = e->n_views;
+    pa.sh_degree = e->settings.sh_degree;
+    pa.band3_compat = e->settings.band3_compat;
+    pa.splats = e->d_splats;
+    pa.offsets = e->d_offsets;
+    pa.desc = e->d_desc_pre;
+    pa.ctl = e->d_ctl;
+    pa.spin_limit = e->settings.spin_limit ? e->settings.spin_limit : kDefaultSpin;
+    pa.never_publish = e->settings.test_never_publish;
+    launch_preprocess(pa, s);
+    mark(1);
+    const uint32_t cap = uint32_t(e->capacity);
+    launch_keygen(e->d_splats, e->d_offsets, e->n, e->d_views, e->n_views, e->d_keys[0], e->d_vals[0], cap, e->d_ctl,
+                  s);
+    mark(2);
+    e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, e->key_bits,
+                                   e->d_desc_sort, e->d_ctl, pa.spin_limit, e->num_sms, s, ev ? ev[3] : nullptr);
+    mark(4);
+    const int b = e->sorted_in_alt ? 1 : 0;
+    launch_tile_ranges(e->d_keys[b], e->total_tiles, e->d_ranges, e->d_ctl, cap, e->num_sms, s);
+    mark(5);
+    BlendArgs ba{};
+    ba.splats = e->d_splats;
+    ba.n = e->n;
+    ba.ctl = e->d_ctl;
+    ba.capacity = cap;
+    ba.vals = e->d_vals[b];
+    ba.ranges = e->d_ranges;
+    ba.views = e->d_views;
+    ba.tile_view = e->n_views > 1 ? e->d_tile_view : nullptr;
+    ba.n_tiles = e->total_tiles;
+    ba.image = e->d_image;
+    ba.image_offset = e->n_views > 1 ? e->d_image_offset : nullptr;
+    ba.final_T = e->d_final_T;
+    ba.n_contrib = e->d_n_contrib;
+    launch_blend(ba, s);
+    mark(6);
+    cudaMemcpyAsync(e->h_stats, e->d_ctl, sizeof(StatsHead), cudaMemcpyDeviceToHost, s);
+}
+
+int run_frame_once(tpd_engine* e, bool use_graph) {
+    if (use_graph) {
+        if (!e->graph_valid) {
+            cudaGraph_t g = nullptr;
+            TPD_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_frame(e);
+            TPD_CUDA(e, cudaStreamEndCapture(e->stream, &g));
+            cudaGraphExec_t ge = nullptr;
+            const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            TPD_CUDA(e, err);
+            e->graph = ge;
+            e->graph_valid = true;
+        }
+        TPD_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
+    } else {
+        enqueue_frame(e);
+        TPD_CUDA(e, cudaGetLastError());
+    }
+    return wait_stream(e);
+}
+
+int set_views_internal(tpd_engine* e, const tpd_view* views, uint32_t nv) {
+    if (nv == 0 || nv > kMaxViews) return fail(e, TPD_ERR_ARG, "view count must be in [1, 256]");
+    bool shape_changed = nv != e->n_views;
+    for (uint32_t v = 0; v < nv && !shape_changed; ++v)
+        shape_changed = views[v].width != e->vw[v] || views[v].height != e->vh[v];
+    for (uint32_t v = 0; v < nv; ++v)
+        if (views[v].width == 0 || views[v].height == 0 || views[v].width > 65536 || views[v].height > 65536)
+            return fail(e, TPD_ERR_ARG, "image size must be in [1, 65536]");
+    uint32_t tiles = 0;
+    uint64_t pixels = 0;
+    std::vector<uint32_t> tile_view;
+    std::vector<uint64_t> img_off(nv);
+    for (uint32_t v = 0; v < nv; ++v) {
+        ViewConst& c = e->h_views[v];
+        std::memcpy(c.view, views[v].view, sizeof(c.view));
+        tpd_mat4_mul(views[v].proj, views[v].view, c.projview);
+        c.focal[0] = views[v].proj[0];
+        c.focal[1] = views[v].proj[5];
+        c.width = views[v].width;
+        c.height = views[v].height;
+        c.tile_base = tiles;
+        const uint32_t t = grid_x(c.width) * grid_y(c.height);
+        if (shape_changed) {
+            tile_view.insert(tile_view.end(), t, v);
+            img_off[v] = pixels;
+        }
+        tiles += t;
+        pixels += uint64_t(c.width) * c.height;
+    }
+    if (!shape_changed) return TPD_OK;
+    invalidate_graph(e);
+    e->frame_valid = false;
+    e->n_views = nv;
+    e->vw.assign(nv, 0);
+    e->vh.assign(nv, 0);
+    for (uint32_t v = 0; v < nv; ++v) {
+        e->vw[v] = views[v].width;
+        e->vh[v] = views[v].height;
+    }
+    e->total_tiles = tiles;
+    e->total_pixels = pixels;
+    e->key_bits = tpd_key_bits_for_tiles(tiles);
+    e->passes = sort_pass_count(e->key_bits);
+    if (pixels > e->pixel_cap) {
+        TPD_CUDA(e, dalloc(e->d_image, pixels * 3));
+        TPD_CUDA(e, dalloc(e->d_final_T, pixels));
+        TPD_CUDA(e, dalloc(e->d_n_contrib, pixels));
+        TPD_CUDA(e, dalloc(e->d_rgba, pixels));
+        e->pixel_cap = pixels;
+    }
+    if (tiles > e->tile_cap) {
+        TPD_CUDA(e, dalloc(e->d_ranges, uint64_t(tiles) * 2));
+        TPD_CUDA(e, dalloc(e->d_tile_view, tiles));
+        e->tile_cap = tiles;
+    }
+    if (!e->d_image_offset) TPD_CUDA(e, dalloc(e->d_image_offset, kMaxViews));
+    TPD_CUDA(e, cudaMemcpy(e->d_tile_view, tile_view.data(), tiles * 4ull, cudaMemcpyHostToDevice));
+    TPD_CUDA(e, cudaMemcpy(e->d_image_offset, img_off.data(), nv * 8ull, cudaMemcpyHostToDevice));
+    return ensure_splat_buffers(e);
+}
+
+int alloc_scene(tpd_engine* e, uint32_t n, uint32_t n_ent) {
+    invalidate_graph(e);
+    e->frame_valid = false;
+    e->n = n;
+    e->n_ent = n_ent ? n_ent : 1;
+    TPD_CUDA(e, dalloc(e->d_recs, uint64_t(n) * kRecordFloats));
+    if (e->h_transforms) cudaFreeHost(e->h_transforms);
+    e->h_transforms = nullptr;
+    TPD_CUDA(e, cudaMallocHost(reinterpret_cast<void**>(&e->h_transforms), sizeof(float) * 16 * e->n_ent));
+    for (uint32_t k = 0; k < e->n_ent; ++k)
+        for (int j = 0; j < 16; ++j) e->h_transforms[k * 16 + j] = (j % 5) == 0 ? 1.f : 0.f;
+    e->identity_transforms = true;
+    TPD_CUDA(e, dalloc(e->d_transforms, uint64_t(e->n_ent) * 16));
+    if (e->n_views) return ensure_splat_buffers(e);
+    return TPD_OK;
+}
+
+void fill_stats(tpd_engine* e, tpd_frame_stats* stats, uint32_t retries) {
+    if (!stats) return;
+    std::memset(stats, 0, sizeof(*stats));
+    stats->keys = e->h_stats->total_keys;
+    stats->key_capacity = e->capacity;
+    stats->visible = e->h_stats->visible;
+    stats->tiles = e->total_tiles;
+    stats->key_bits = e->key_bits;
+    stats->sort_passes = e->passes;
+    stats->status = e->h_stats->status;
+    stats->retries = retries;
+    stats->views = e->n_views;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tpd_version(void) { return "tpdsplat 0.1 (sm_103a)"; }
+
+const char* tpd_status_string(int s) {
+    switch (s) {
+        case TPD_OK: return "ok";
+        case TPD_ERR_ARG: return "invalid argument";
+        case TPD_ERR_OOM: return "out of device memory";
+        case TPD_ERR_TIMEOUT: return "timeout";
+        case TPD_ERR_DEVICE: return "device error";
+        case TPD_ERR_STATE: return "invalid state";
+        case TPD_ERR_CAPACITY: return "capacity exceeded";
+        case TPD_ERR_IO: return "i/o error";
+        default: return "unknown";
+    }
+}
+
+void tpd_settings_init(tpd_settings* s) {
+    if (!s) return;
+    std::memset(s, 0, sizeof(*s));
+    s->sh_degree = 3;
+    s->band3_compat = 1;
+    s->device = 0;
+    s->use_graph = 1;
+    s->timeout_s = 60.0;
+}
+
+int tpd_create(const tpd_settings* s, tpd_engine** out) {
+    if (!out) return TPD_ERR_ARG;
+    *out = nullptr;
+    tpd_engine* e = new tpd_engine();
+    if (s) e->settings = *s;
+    else tpd_settings_init(&e->settings);
+    if (e->settings.sh_degree > 3) e->settings.sh_degree = 3;  // GaussianEngine.cpp:366-370
+    e->device = e->settings.device;
+    auto bail = [&](int code) {
+        tpd_destroy(e);
+        return code;
+    };
+    if (cudaSetDevice(e->device) != cudaSuccess) return bail(TPD_ERR_DEVICE);
+    cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device);
+    if (e->settings.stream) {
+        e->stream = static_cast<cudaStream_t>(e->settings.stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(TPD_ERR_DEVICE);
+        e->own_stream = true;
+    }
+    if (cudaEventCreateWithFlags(&e->done_event, cudaEventDisableTiming) != cudaSuccess) return bail(TPD_ERR_DEVICE);
+    if (cudaMalloc(&e->d_ctl, sizeof(FrameCtl)) != cudaSuccess) return bail(TPD_ERR_OOM);
+    if (cudaMemset(e->d_ctl, 0, sizeof(FrameCtl)) != cudaSuccess) return bail(TPD_ERR_DEVICE);
+    if (cudaMallocHost(reinterpret_cast<void**>(&e->h_stats), sizeof(StatsHead)) != cudaSuccess) return bail(TPD_ERR_OOM);
+    if (cudaMallocHost(reinterpret_cast<void**>(&e->h_views), sizeof(ViewConst) * kMaxViews) != cudaSuccess)
+        return bail(TPD_ERR_OOM);
+    std::memset(e->h_views, 0, sizeof(ViewConst) * kMaxViews);
+    if (cudaMalloc(&e->d_views, sizeof(ViewConst) * kMaxViews) != cudaSuccess) return bail(TPD_ERR_OOM);
+    if (e->settings.initial_key_capacity) {
+        if (ensure_key_capacity(e, e->settings.initial_key_capacity) != TPD_OK) return bail(TPD_ERR_OOM);
+    }
+    *out = e;
+    return TPD_OK;
+}
+
+void tpd_destroy(tpd_engine* e) {
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    invalidate_graph(e);
+    dfree(e->d_recs);
+    dfree(e->d_ent_idx);
+    dfree(e->d_transforms);
+    dfree(e->d_views);
+    dfree(e->d_tile_view);
+    dfree(e->d_image_offset);
+    dfree(e->d_splats);
+    dfree(e->d_offsets);
+    dfree(e->d_desc_pre);
+    dfree(e->d_ent_mats);
+    for (int b = 0; b < 2; ++b) {
+        dfree(e->d_keys[b]);
+        dfree(e->d_vals[b]);
+    }
+    dfree(e->d_desc_sort);
+    dfree(e->d_ranges);
+    dfree(e->d_image);
+    dfree(e->d_final_T);
+    dfree(e->d_n_contrib);
+    dfree(e->d_rgba);
+    dfree(e->d_g2d);
+    dfree(e->d_gscratch);
+    dfree(e->d_ctl);
+    if (e->h_stats) cudaFreeHost(e->h_stats);
+    if (e->h_views) cudaFreeHost(e->h_views);
+    if (e->h_transforms) cudaFreeHost(e->h_transforms);
+    if (e->done_event) cudaEventDestroy(e->done_event);
+    for (int i = 0; i < tpd_engine::kTimingSlots; ++i)
+        for (int k = 0; k < tpd_engine::kTimingEvents; ++k)
+            if (e->tev[i][k]) cudaEventDestroy(e->tev[i][k]);
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+const char* tpd_last_error(const tpd_engine* e) { return e ? e->last_error.c_str() : "no engine"; }
+
+int tpd_compile(tpd_engine* e, const void* records, uint32_t n, const uint32_t* entity_index, uint32_t n_entities) {
+    if (!e) return TPD_ERR_ARG;
+    if (n > 0 && !records) return fail(e, TPD_ERR_ARG, "records is NULL");
+    if (n_entities == 0) n_entities = 1;
+    if (entity_index) {
+        for (uint32_t i = 0; i < n; ++i)
+            if (entity_index[i] >= n_entities) return fail(e, TPD_ERR_ARG, "entity index out of range");
+    }
+    cudaSetDevice(e->device);
+    int rc = alloc_scene(e, n, n_entities);
+    if (rc != TPD_OK) return rc;
+    if (n) TPD_CUDA(e, cudaMemcpy(e->d_recs, records, uint64_t(n) * kRecordBytes, cudaMemcpyHostToDevice));
+    if (entity_index && n) {
+        TPD_CUDA(e, dalloc(e->d_ent_idx, n));
+        TPD_CUDA(e, cudaMemcpy(e->d_ent_idx, entity_index, n * 4ull, cudaMemcpyHostToDevice));
+    } else {
+        dfree(e->d_ent_idx);
+    }
+    e->compiled = true;
+    return TPD_OK;
+}
+
+int tpd_compile_params_device(tpd_engine* e, const float* means, const float* log_scales, const float* quats,
+                              const float* opacity_logits, const float* sh, uint32_t n) {
+    if (!e) return TPD_ERR_ARG;
+    if (n > 0 && (!means || !log_scales || !quats || !opacity_logits || !sh))
+        return fail(e, TPD_ERR_ARG, "parameter pointer is NULL");
+    cudaSetDevice(e->device);
+    int rc = alloc_scene(e, n, 1);
+    if (rc != TPD_OK) return rc;
+    dfree(e->d_ent_idx);
+    launch_pack_records(means, log_scales, quats, opacity_logits, sh, n, e->d_recs, e->stream);
+    TPD_CUDA(e, cudaGetLastError());
+    TPD_CUDA(e, cudaStreamSynchronize(e->stream));
+    e->compiled = true;
+    return TPD_OK;
+}
+
+int tpd_set_transform(tpd_engine* e, uint32_t entity, const float model[16]) {
+    if (!e || !model) return TPD_ERR_ARG;
+    if (!e->compiled) return fail(e, TPD_ERR_STATE, "set_transform before compile");
+    if (entity >= e->n_ent) return TPD_OK;  // unknown entities are ignored (TransformHost.cpp:4-6)
+    std::memcpy(e->h_transforms + entity * 16, model, 64);
+    if (e->identity_transforms) invalidate_graph(e);  // the frame gains a transform upload
+    e->identity_transforms = false;
+    return TPD_OK;
+}
+
+int tpd_set_camera(tpd_engine* e, const float view[16], const float proj[16], uint32_t width, uint32_t height) {
+    if (!e || !view || !proj) return TPD_ERR_ARG;
+    tpd_view v;
+    std::memcpy(v.view, view, 64);
+    std::memcpy(v.proj, proj, 64);
+    v.width = width;
+    v.height = height;
+    cudaSetDevice(e->device);
+    return set_views_internal(e, &v, 1);
+}
+
+int tpd_set_views(tpd_engine* e, const tpd_view* views, uint32_t n_views) {
+    if (!e || !views) return TPD_ERR_ARG;
+    cudaSetDevice(e->device);
+    return set_views_internal(e, views, n_views);
+}
+
+int tpd_raster_frame(tpd_engine* e, tpd_frame_stats* stats) {
+    if (!e) return TPD_ERR_ARG;
+    if (!e->compiled) return fail(e, TPD_ERR_STATE, "raster_frame before compile");
+    if (!e->n_views) return fail(e, TPD_ERR_STATE, "raster_frame before set_camera");
+    cudaSetDevice(e->device);
+    int rc = ensure_splat_buffers(e);
+    if (rc != TPD_OK) return rc;
+    if (e->capacity == 0) {
+        rc = ensure_key_capacity(e, std::max<uint64_t>(uint64_t(e->n) * e->n_views * 4, 1u << 20));
+        if (rc != TPD_OK) return rc;
+    }
+    uint32_t retries = 0;
+    e->frame_valid = false;
+    while (true) {
+        // the first frame after any reallocation runs eagerly; later ones replay the graph
+        const bool graph = e->settings.use_graph && !e->settings.stage_timing && !e->needs_eager && retries == 0;
+        rc = run_frame_once(e, graph);
+        if (rc != TPD_OK) return rc;
+        if (!graph) e->needs_eager = false;
+        const StatsHead h = *e->h_stats;
+        if (h.status & kStatusKeyOverflow) {
+            if (retries >= 3) return fail(e, TPD_ERR_CAPACITY, "key buffers kept overflowing");
+            rc = ensure_key_capacity(e, uint64_t(h.total_keys) + uint64_t(h.total_keys) / 4 + 1024);
+            if (rc != TPD_OK) return rc;
+            ++retries;
+            continue;
+        }
+        if (h.status & (kStatusLookbackTimeout | kStatusMbarTimeout)) {
+            e->frames++;
+            return fail(e, TPD_ERR_TIMEOUT, "a bounded device wait ran out (status " + std::to_string(h.status) + ")");
+        }
+        break;
+    }
+    e->frames++;
+    e->frame_valid = true;
+    if (e->settings.stage_timing) harvest_all(e);
+    fill_stats(e, stats, retries);
+    return TPD_OK;
+}
+
+int tpd_raster_frames_async(tpd_engine* e, uint32_t count) {
+    if (!e) return TPD_ERR_ARG;
+    if (!e->frame_valid || e->needs_eager)
+        return fail(e, TPD_ERR_STATE, "render one frame with tpd_raster_frame after any change first");
+    cudaSetDevice(e->device);
+    const bool graph = e->settings.use_graph && !e->settings.stage_timing;
+    if (graph && !e->graph_valid) {
+        cudaGraph_t g = nullptr;
+        TPD_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_frame(e);
+        TPD_CUDA(e, cudaStreamEndCapture(e->stream, &g));
+        cudaGraphExec_t ge = nullptr;
+        const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        TPD_CUDA(e, err);
+        e->graph = ge;
+        e->graph_valid = true;
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        if (graph) TPD_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
+        else enqueue_frame(e);
+    }
+    TPD_CUDA(e, cudaGetLastError());
+    e->frames += count;
+    return TPD_OK;
+}
+
+int tpd_sync(tpd_engine* e, tpd_frame_stats* stats) {
+    if (!e) return TPD_ERR_ARG;
+    cudaSetDevice(e->device);
+    int rc = wait_stream(e);
+    if (rc != TPD_OK) return rc;
+    if (e->settings.stage_timing) harvest_all(e);
+    const StatsHead h = *e->h_stats;
+    fill_stats(e, stats, 0);
+    if (h.status & kStatusKeyOverflow) {
+        e->frame_valid = false;
+        return fail(e, TPD_ERR_CAPACITY, "keys outgrew the key buffers; render with tpd_raster_frame");
+    }
+    if (h.status & kStatusFatal) return fail(e, TPD_ERR_TIMEOUT, "a bounded device wait ran out");
+    return TPD_OK;
+}
+
+int tpd_stage_times(tpd_engine* e, double* ms, uint64_t* frames, int reset) {
+    if (!e) return TPD_ERR_ARG;
+    cudaSetDevice(e->device);
+    harvest_all(e);
+    if (ms) for (int k = 0; k < TPD_STAGE_COUNT; ++k) ms[k] = e->stage_ms[k];
+    if (frames) *frames = e->timed_frames;
+    if (reset) {
+        for (int k = 0; k < TPD_STAGE_COUNT; ++k) e->stage_ms[k] = 0.0;
+        e->timed_frames = 0;
+    }
+    return TPD_OK;
+}
+
+int tpd_read_image(tpd_engine* e, void* dst, uint32_t format, int dst_is_device) {
+    if (!e || !dst) return TPD_ERR_ARG;
+    if (!e->frame_valid) return fail(e, TPD_ERR_STATE, "no rendered frame");
+    cudaSetDevice(e->device);
+    const cudaMemcpyKind kind = dst_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (format == TPD_IMAGE_RGB32F) {
+        TPD_CUDA(e, cudaMemcpyAsync(dst, e->d_image, e->total_pixels * 12, kind, e->stream));
+    } else if (format == TPD_IMAGE_RGBA8) {
+        launch_pack_rgba8(e->d_image, e->d_rgba, e->total_pixels, e->stream);
+        TPD_CUDA(e, cudaGetLastError());
+        TPD_CUDA(e, cudaMemcpyAsync(dst, e->d_rgba, e->total_pixels * 4, kind, e->stream));
+    } else {
+        return fail(e, TPD_ERR_ARG, "unknown image format");
+    }
+    return wait_stream(e);
+}
+
+int tpd_backward(tpd_engine* e, const float* dL_dimage, float* g_means, float* g_log_scales, float* g_quats,
+                 float* g_logits, float* g_sh) {
+    if (!e || !dL_dimage) return TPD_ERR_ARG;
+    if (!e->frame_valid) return fail(e, TPD_ERR_STATE, "backward before a rendered frame");
+    cudaSetDevice(e->device);
+    const uint64_t g2d = uint64_t(e->n) * e->n_views * 9;
+    if (g2d > e->g2d_cap) {
+        TPD_CUDA(e, dalloc(e->d_g2d, g2d));
+        e->g2d_cap = g2d;
+    }
+    const uint64_t gs = uint64_t(e->n) * (3 + 3 + 4 + 1 + 48);
+    if ((!g_means || !g_log_scales || !g_quats || !g_logits || !g_sh) && gs > e->gscratch_cap) {
+        TPD_CUDA(e, dalloc(e->d_gscratch, gs));
+        e->gscratch_cap = gs;
+    }
+    float* sc = e->d_gscratch;
+    const uint64_t n = e->n;
+    if (!g_means) g_means = sc;
+    if (!g_log_scales) g_log_scales = sc + n * 3;
+    if (!g_quats) g_quats = sc + n * 6;
+    if (!g_logits) g_logits = sc + n * 10;
+    if (!g_sh) g_sh = sc + n * 11;
+    TPD_CUDA(e, cudaMemsetAsync(e->d_g2d, 0, g2d * 4, e->stream));
+    const int b = e->sorted_in_alt ? 1 : 0;
+    BlendBackwardArgs bb{};
+    bb.splats = e->d_splats;
+    bb.n = e->n;
+    bb.ctl = e->d_ctl;
+    bb.capacity = uint32_t(e->capacity);
+    bb.vals = e->d_vals[b];
+    bb.ranges = e->d_ranges;
+    bb.views = e->d_views;
+    bb.tile_view = e->n_views > 1 ? e->d_tile_view : nullptr;
+    bb.n_tiles = e->total_tiles;
+    bb.image_offset = e->n_views > 1 ? e->d_image_offset : nullptr;
+    bb.final_T = e->d_final_T;
+    bb.n_contrib = e->d_n_contrib;
+    bb.dL_dimage = dL_dimage;
+    bb.g2d = e->d_g2d;
+    bb.g2d_stride = 9;
+    bb.g2d_view_stride = uint64_t(e->n) * 9;
+    launch_blend_backward(bb, e->stream);
+    PreprocessBackwardArgs pb{};
+    pb.recs = e->d_recs;
+    pb.n = e->n;
+    pb.ent_idx = e->d_ent_idx;
+    pb.ent_mats = e->d_ent_mats;
+    pb.n_ent = e->n_ent;
+    pb.views = e->d_views;
+    pb.n_views = e->n_views;
+    pb.sh_degree = e->settings.sh_degree;
+    pb.band3_compat = e->settings.band3_compat;
+    pb.splats = e->d_splats;
+    pb.g2d = e->d_g2d;
+    pb.g_means = g_means;
+    pb.g_log_scales = g_log_scales;
+    pb.g_quats = g_quats;
+    pb.g_logits = g_logits;
+    pb.g_sh = g_sh;
+    launch_preprocess_backward(pb, e->stream);
+    TPD_CUDA(e, cudaGetLastError());
+    return wait_stream(e);
+}
+
+int tpd_get_buffer(const tpd_engine* e, uint32_t which, void** ptr, uint64_t* bytes) {
+    if (!e || !ptr) return TPD_ERR_ARG;
+    const int b = e->sorted_in_alt ? 1 : 0;
+    void* p = nullptr;
+    uint64_t sz = 0;
+    const uint64_t vn = uint64_t(e->n) * e->n_views;
+    switch (which) {
+        case TPD_BUF_RECORDS: p = e->d_recs; sz = uint64_t(e->n) * kRecordBytes; break;
+        case TPD_BUF_SPLATS: p = e->d_splats; sz = vn * sizeof(Splat); break;
+        case TPD_BUF_OFFSETS: p = e->d_offsets; sz = vn * 4; break;
+        case TPD_BUF_KEYS: p = e->d_keys[b]; sz = e->capacity * 8; break;
+        case TPD_BUF_VALUES: p = e->d_vals[b]; sz = e->capacity * 4; break;
+        case TPD_BUF_RANGES: p = e->d_ranges; sz = uint64_t(e->total_tiles) * 8; break;
+        case TPD_BUF_IMAGE: p = e->d_image; sz = e->total_pixels * 12; break;
+        case TPD_BUF_FINAL_T: p = e->d_final_T; sz = e->total_pixels * 4; break;
+        case TPD_BUF_N_CONTRIB: p = e->d_n_contrib; sz = e->total_pixels * 4; break;
+        case TPD_BUF_G2D: p = e->d_g2d; sz = vn * 9 * 4; break;
+        default: return TPD_ERR_ARG;
+    }
+    *ptr = p;
+    if (bytes) *bytes = sz;
+    return TPD_OK;
+}
+
+int tpd_read_buffer(tpd_engine* e, uint32_t which, void* dst, uint64_t offset, uint64_t bytes, int dst_is_device) {
+    if (!e || !dst) return TPD_ERR_ARG;
+    void* p = nullptr;
+    uint64_t sz = 0;
+    int rc = tpd_get_buffer(e, which, &p, &sz);
+    if (rc != TPD_OK) return rc;
+    if (offset + bytes > sz || !p) return fail(e, TPD_ERR_ARG, "read past the end of the buffer");
+    cudaSetDevice(e->device);
+    TPD_CUDA(e, cudaMemcpyAsync(dst, static_cast<char*>(p) + offset, bytes,
+                                dst_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, e->stream));
+    return wait_stream(e);
+}
+
+void* tpd_get_stream(const tpd_engine* e) { return e ? static_cast<void*>(e->stream) : nullptr; }
+
+// ---- stage entry points
+
+size_t tpd_sort_workspace_size(uint32_t n) {
+    return 256 * ((sizeof(FrameCtl) + 255) / 256) + sort_desc_entries(n) * 8;
+}
+
+int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t n,
+                   uint32_t key_bits, void* workspace, size_t workspace_bytes, void* stream, int* result_in_alt) {
+    if (!result_in_alt) return TPD_ERR_ARG;
+    *result_in_alt = 0;
+    if (n == 0) return TPD_OK;
+    if (!keys || !vals || !keys_alt || !vals_alt || !workspace) return TPD_ERR_ARG;
+    if (key_bits == 0 || key_bits > 64 || n > 0x7FFFFFFFu) return TPD_ERR_ARG;
+    if (workspace_bytes < tpd_sort_workspace_size(n)) return TPD_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    FrameCtl* ctl = static_cast<FrameCtl*>(workspace);
+    uint64_t* desc = reinterpret_cast<uint64_t*>(static_cast<char*>(workspace) + 256 * ((sizeof(FrameCtl) + 255) / 256));
+    int sms = 148, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaMemsetAsync(desc, 0, sort_desc_entries(n) * 8, s) != cudaSuccess) return TPD_ERR_DEVICE;
+    launch_sort_begin(ctl, n, s);
+    const bool alt = launch_sort(keys, vals, keys_alt, vals_alt, n, key_bits, desc, ctl, kDefaultSpin, sms, s);
+    *result_in_alt = alt ? 1 : 0;
+    return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;
+}
+
+size_t tpd_scan_workspace_size(uint32_t n) {
+    return 256 * ((sizeof(FrameCtl) + 255) / 256) + (size_t(n) / kScanTileStandalone + 2) * 8;
+}
+
+int tpd_scan_tiles(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+    if (!total || !workspace) return TPD_ERR_ARG;
+    if (n > 0 && (!splats || !offsets)) return TPD_ERR_ARG;
+    if (workspace_bytes < tpd_scan_workspace_size(n)) return TPD_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    FrameCtl* ctl = static_cast<FrameCtl*>(workspace);
+    uint64_t* desc = reinterpret_cast<uint64_t*>(static_cast<char*>(workspace) + 256 * ((sizeof(FrameCtl) + 255) / 256));
+    const size_t entries = size_t(n) / kScanTileStandalone + 2;
+    if (cudaMemsetAsync(desc, 0, entries * 8, s) != cudaSuccess) return TPD_ERR_DEVICE;
+    launch_sort_begin(ctl, 0, s);
+    launch_scan_tiles(static_cast<const Splat*>(splats), n, offsets, desc, ctl, kDefaultSpin, 0, s);
+    if (cudaMemcpyAsync(total, &ctl->total_keys, 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TPD_ERR_DEVICE;
+    return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+// keygen.cu — kernel (b, second half): key duplication, and kernel (d): tile ranges.
+//
+// Reference: keygen.slang:23-53 (one thread per Gaussian looping over its tile
+// rect) and range.slang:18-35 (+ fillBuffer, GaussianEngine.cpp:843-848).
+//
+// GB300 form of keygen: a warp owns 32 consecutive Gaussians and expands their
+// keys cooperatively. Lane s of each step writes output slot s of the warp's
+// contiguous key range, finding its Gaussian by a 5-step shuffle search over
+// the warp's exclusive offsets, so stores are fully coalesced and one large
+// Gaussian no longer serialises its warp. Keys and values are bit-identical to
+// the reference's: same rect arithmetic, same row-major order, same offsets.
+#include "tpd_common.cuh"
+#include "tpd_kernels.h"
+#include "tpd_scan.cuh"
+
+namespace tpd {
+namespace {
+
+constexpr uint32_t kKeygenThreads = 256;
+
+__global__ void __launch_bounds__(kKeygenThreads)
+    keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ offsets, uint32_t n,
+                  const ViewConst* __restrict__ views, uint32_t n_views, uint64_t* __restrict__ keys,
+                  uint32_t* __restrict__ vals, uint32_t capacity, FrameCtl* ctl) {
+    const uint32_t lane = lane_id();
+    const uint32_t warps_total = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
+    const uint32_t wpv = (n + 31) / 32;  // warps per view; a warp never straddles a view or a 128-partition
+    if (ctl->status & kStatusFatal) return;
+
+    for (uint32_t wi = warp_global; wi < wpv * n_views; wi += warps_total) {
+        const uint32_t v = wi / wpv;
+        const uint32_t g0 = (wi % wpv) * 32u;
+        const uint32_t gx = grid_x(views[v].width), gy = grid_y(views[v].height);
+        const uint32_t tile_base = views[v].tile_base;
+        const size_t vbase = size_t(v) * n;
+        const uint32_t i = g0 + lane;
+        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0, off = 0, depth_bits = 0;
+        if (i < n) {
+            const float4 texel = reinterpret_cast<const float4*>(splats + vbase + i)[1];  // px, py, viewZ, radius
+            off = offsets[vbase + i];
+            if (texel.w > 0.0f) {
+                bounding_rect(texel.x, texel.y, texel.w, gx, gy, x0, y0, x1, y1);
+                depth_bits = __float_as_uint(texel.z);
+            }
+        }
+        const uint32_t w = x1 - x0;
+        const uint32_t cnt = w * (y1 - y0);
+        const uint32_t incl = warp_inclusive_scan(cnt);
+        const uint32_t excl = incl - cnt;
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const uint32_t base = __shfl_sync(0xFFFFFFFFu, off, 0);
+        for (uint32_t s0 = 0; s0 < total; s0 += 32u) {
+            const uint32_t s = s0 + lane;
+            // owner: the largest lane j with excl_j <= s
+            uint32_t j = 0;
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1) {
+                const uint32_t cand = j + step;
+                const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, cand & 31u);
+                if (cand < 32u && e <= s) j = cand;
+            }
+            const uint32_t jx0 = __shfl_sync(0xFFFFFFFFu, x0, j);
+            const uint32_t jy0 = __shfl_sync(0xFFFFFFFFu, y0, j);
+            const uint32_t jw = __shfl_sync(0xFFFFFFFFu, w, j);
+            const uint32_t jex = __shfl_sync(0xFFFFFFFFu, excl, j);
+            const uint32_t jdb = __shfl_sync(0xFFFFFFFFu, depth_bits, j);
+            if (s < total) {
+                const uint32_t local = s - jex;
+                const uint32_t ty = jy0 + local / jw;
+                const uint32_t tx = jx0 + local % jw;
+                const uint64_t pos = uint64_t(base) + s;
+                if (pos < capacity) {
+                    keys[pos] = (uint64_t(tile_base + ty * gx + tx) << 32) | uint64_t(jdb);
+                    vals[pos] = g0 + j;
+                }
+            }
+        }
+    }
+}
+
+// range.slang:18-35 over K = min(total_keys, capacity) keys; ranges zeroed first.
+__global__ void tile_ranges_kernel(const uint64_t* __restrict__ keys, uint32_t* __restrict__ ranges,
+                                   uint32_t n_tiles, const FrameCtl* ctl, uint32_t capacity) {
+    if (ctl->status & kStatusFatal) return;
+    const uint32_t K = min(ctl->total_keys, capacity);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < K; idx += stride) {
+        const uint32_t cur = uint32_t(keys[idx] >> 32);
+        if (cur >= n_tiles) continue;  // only reachable with corrupted keys
+        if (idx == 0) {
+            ranges[cur * 2 + 0] = 0;
+        } else {
+            const uint32_t prev = uint32_t(keys[idx - 1] >> 32);
+            if (cur != prev) {
+                if (prev < n_tiles) ranges[prev * 2 + 1] = idx;
+                ranges[cur * 2 + 0] = idx;
+            }
+        }
+        if (idx == K - 1) ranges[cur * 2 + 1] = idx + 1;
+    }
+}
+
+}  // namespace
+
+void launch_keygen(const Splat* splats, const uint32_t* offsets, uint32_t n, const ViewConst* views,
+                   uint32_t n_views, uint64_t* keys, uint32_t* vals, uint32_t capacity, FrameCtl* ctl,
+                   cudaStream_t s) {
+    if (n == 0 || n_views == 0) return;
+    const uint64_t warps = uint64_t((n + 31) / 32) * n_views;
+    uint64_t blocks = (warps * 32 + kKeygenThreads - 1) / kKeygenThreads;
+    blocks = blocks < 8192u ? blocks : 8192u;
+    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, offsets, n, views, n_views, keys, vals,
+                                                              capacity, ctl);
+}
+
+void launch_tile_ranges(const uint64_t* keys, uint32_t n_tiles, uint32_t* ranges, FrameCtl* ctl, uint32_t capacity,
+                        int num_sms, cudaStream_t s) {
+    cudaMemsetAsync(ranges, 0, size_t(n_tiles) * 8, s);
+    const int blocks = (num_sms > 0 ? num_sms : 148) * 8;
+    tile_ranges_kernel<<<blocks, 256, 0, s>>>(keys, ranges, n_tiles, ctl, capacity);
+}
+
+}  // namespace tpd

@@ -1,0 +1,425 @@
+// preprocess.cu — kernel (a): per-Gaussian projection to a 48-byte Splat,
+// with the tile-count exclusive scan (b, first half) fused in.
+//
+// Reference: project.slang:33-107 with splat/common.slang (SH, frustum test,
+// camera position) and splat/volume.slang (ndc2pix, bounding rect, 3D
+// covariance, EWA projection, Jacobian); prefix.slang:40-158 for the scan.
+//
+// GB300 layout: a CTA of 128 threads owns 128 consecutive records (30,720 B).
+// One elected thread stages them with a single TMA bulk copy into shared
+// memory; threads then read their record with conflict-free 16-byte loads
+// (record stride 60 words). The CTA's partition id comes from an atomic
+// ticket, so the fused decoupled look-back only ever waits on CTAs that
+// started earlier. Arithmetic follows the shader source left to right with
+// matrix products accumulated k = 0..n-1; this file is compiled with
+// --fmad=false so no product is fused into an add.
+#include "tpd_common.cuh"
+#include "tpd_kernels.h"
+#include "tpd_scan.cuh"
+
+namespace tpd {
+namespace {
+
+constexpr uint32_t kPreThreads = 128;
+
+// SH constants (splat/common.slang:3-20).
+__constant__ float cSH_C0 = 0.28209479177387814f;
+__constant__ float cSH_C1 = 0.4886025119029199f;
+__constant__ float cSH_C2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f,
+                                -1.0925484305920792f, 0.5462742152960396f};
+__constant__ float cSH_C3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570457994644658f,
+                                0.3731763325901154f, -0.4570457994644658f, 1.445305721320277f,
+                                -0.5900435899266435f};
+
+__device__ __forceinline__ void mat4mul(const float* A, const float* B, float* C) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            C[i * 4 + j] = A[i * 4 + 0] * B[0 * 4 + j] + A[i * 4 + 1] * B[1 * 4 + j] +
+                           A[i * 4 + 2] * B[2 * 4 + j] + A[i * 4 + 3] * B[3 * 4 + j];
+}
+
+__device__ __forceinline__ void mat3mul(const float* A, const float* B, float* C) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            C[i * 3 + j] = A[i * 3 + 0] * B[0 * 3 + j] + A[i * 3 + 1] * B[1 * 3 + j] + A[i * 3 + 2] * B[2 * 3 + j];
+}
+
+__device__ __forceinline__ void mat3T(const float* A, float* B) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) B[j * 3 + i] = A[i * 3 + j];
+}
+
+// frame_begin: one CTA. Clears tickets / sort histograms, advances the tag and
+// computes per-entity view*model and projview*model (the products of
+// passFrustumClipping, common.slang:102,106, hoisted out of the per-Gaussian loop;
+// identical values since they do not depend on the Gaussian).
+__global__ void frame_begin_kernel(FrameCtl* ctl, const float* transforms, uint32_t n_ent, const ViewConst* views,
+                                   uint32_t n_views, float* ent_mats) {
+    const uint32_t t = threadIdx.x;
+    for (uint32_t i = t; i < 16; i += blockDim.x) ctl->ticket[i] = 0;
+    for (uint32_t i = t; i < 8 * 256; i += blockDim.x) (&ctl->sort_hist[0][0])[i] = 0;
+    if (t == 0) {
+        ctl->tag = ctl->tag + 1;
+        ctl->status = 0;
+        ctl->total_keys = 0;
+        ctl->visible = 0;
+    }
+    if (!views || !ent_mats) return;
+    for (uint32_t ve = t; ve < n_views * n_ent; ve += blockDim.x) {
+        const uint32_t v = ve / n_ent, e = ve % n_ent;
+        float M[16];
+        if (transforms) {
+            for (int k = 0; k < 16; ++k) M[k] = transforms[size_t(e) * 16 + k];
+        } else {
+            for (int k = 0; k < 16; ++k) M[k] = (k % 5) == 0 ? 1.0f : 0.0f;
+        }
+        float V[16], P[16], VM[16], PM[16];
+        for (int k = 0; k < 16; ++k) { V[k] = views[v].view[k]; P[k] = views[v].projview[k]; }
+        mat4mul(V, M, VM);
+        mat4mul(P, M, PM);
+        float* o = ent_mats + size_t(ve) * kEntityMatFloats;
+        for (int k = 0; k < 12; ++k) o[k] = VM[k];
+        for (int k = 0; k < 16; ++k) o[12 + k] = PM[k];
+    }
+}
+
+// Reads float k of a record staged in shared memory.
+struct Rec {
+    const float* p;
+    __device__ __forceinline__ float operator[](int k) const { return p[k]; }
+    __device__ __forceinline__ float4 f4(int q) const { return reinterpret_cast<const float4*>(p)[q]; }
+};
+
+// project() for one Gaussian. Returns the tile count (0 when culled) and fills s.
+__device__ __forceinline__ uint32_t project_one(const Rec& rec, const float* em, const ViewConst& v,
+                                                uint32_t deg, bool compat, Splat& s) {
+    s = Splat{0.f, 0.f, 0.f, 0u, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const float4 pos_op = rec.f4(0);
+    const float mean[3] = {pos_op.x, pos_op.y, pos_op.z};
+
+    // passFrustumClipping (common.slang:98-119)
+    float vp[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        vp[i] = em[i * 4 + 0] * mean[0] + em[i * 4 + 1] * mean[1] + em[i * 4 + 2] * mean[2] + em[i * 4 + 3] * 1.0f;
+    if (vp[2] <= 0.0f) return 0;
+    float cp[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        cp[i] = em[12 + i * 4 + 0] * mean[0] + em[12 + i * 4 + 1] * mean[1] + em[12 + i * 4 + 2] * mean[2] +
+                em[12 + i * 4 + 3] * 1.0f;
+    const float k13 = 1.3f;
+    if (cp[0] < -k13 * cp[3] || cp[0] > k13 * cp[3]) return 0;
+    if (cp[1] < -k13 * cp[3] || cp[1] > k13 * cp[3]) return 0;
+    if (cp[2] < 0.0f || cp[2] > cp[3]) return 0;
+    const float inv_w = 1.0f / cp[3];
+    const float ndc_x = cp[0] * inv_w, ndc_y = cp[1] * inv_w;
+
+    // focal = 0.5 * imageSize * focalNDC (project.slang:55)
+    const float fx = (0.5f * float(v.width)) * v.focal[0];
+    const float fy = (0.5f * float(v.height)) * v.focal[1];
+
+    // computeCovariance (volume.slang:20-41)
+    const float4 q = rec.f4(1), sc = rec.f4(2);
+    const float S[9] = {sc.x * sc.w, 0.f, 0.f, 0.f, sc.y * sc.w, 0.f, 0.f, 0.f, sc.z * sc.w};
+    const float x = q.x, y = q.y, z = q.z, w = q.w;
+    const float R[9] = {1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y - w * z), 2.0f * (x * z + w * y),
+                        2.0f * (x * y + w * z), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z - w * x),
+                        2.0f * (x * z - w * y), 2.0f * (y * z + w * x), 1.0f - 2.0f * (x * x + y * y)};
+    float sigma[9], sigmaT[9], cov3[9];
+    mat3mul(R, S, sigma);
+    mat3T(sigma, sigmaT);
+    mat3mul(sigma, sigmaT, cov3);
+
+    // projectCovariance + computeJacobian (volume.slang:44-63)
+    const float W3[9] = {v.view[0], v.view[1], v.view[2], v.view[4], v.view[5],
+                         v.view[6], v.view[8], v.view[9], v.view[10]};
+    const float f0 = fx / vp[2], f1 = fy / vp[2];
+    const float t0 = vp[0] / vp[2], t1 = vp[1] / vp[2];
+    const float J[9] = {f0, 0.f, -f0 * t0, 0.f, f1, -f1 * t1, 0.f, 0.f, 0.f};
+    float Tm[9], TmT[9], inner[9], cov2[9];
+    mat3mul(J, W3, Tm);
+    mat3T(Tm, TmT);
+    mat3mul(cov3, TmT, inner);
+    mat3mul(Tm, inner, cov2);
+
+    // low-pass filter and inverse (project.slang:60-66)
+    const float ca = cov2[0] + 0.3f, cb = cov2[3], cc = cov2[4] + 0.3f;
+    const float det = ca * cc - cb * cb;
+    if (det == 0.0f) return 0;
+    const float det_inv = 1.0f / det;
+    const float conic0 = cc * det_inv, conic1 = -cb * det_inv, conic2 = ca * det_inv;
+
+    // screen-space extent (project.slang:69-72)
+    const float mid = 0.5f * (ca + cc);
+    const float l1 = mid + sqrtf(fmaxf(0.1f, mid * mid - det));
+    const float l2 = mid - sqrtf(fmaxf(0.1f, mid * mid - det));
+    const float radius = ceilf(3.0f * sqrtf(fmaxf(l1, l2)));
+
+    // ndc2pix (volume.slang:3-8) and getBoundingRect
+    const float px = ((ndc_x + 1.0f) * float(v.width) - 1.0f) * 0.5f;
+    const float py = ((ndc_y + 1.0f) * float(v.height) - 1.0f) * 0.5f;
+    uint32_t x0, y0, x1, y1;
+    bounding_rect(px, py, radius, grid_x(v.width), grid_y(v.height), x0, y0, x1, y1);
+    const uint32_t touched = (x1 - x0) * (y1 - y0);
+    if (touched == 0) return 0;
+
+    // camera position (common.slang:88-92) and view direction from the pre-model mean
+    float campos[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        campos[i] = -(v.view[0 * 4 + i] * v.view[0 * 4 + 3] + v.view[1 * 4 + i] * v.view[1 * 4 + 3] +
+                      v.view[2 * 4 + i] * v.view[2 * 4 + 3]);
+    const float d0 = mean[0] - campos[0], d1 = mean[1] - campos[1], d2 = mean[2] - campos[2];
+    const float len = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+    const float dx = d0 / len, dy = d1 / len, dz = d2 / len;
+
+    // evaluateSphericalHarmonics (common.slang:35-80)
+    float res[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) res[c] = cSH_C0 * rec[12 + c];
+    if (deg > 0) {
+        auto F = [&](int idx, int c) { return rec[12 + (idx - 1) + c * 15 + 3]; };
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            res[c] = res[c] - (cSH_C1 * dy) * F(1, c) + (cSH_C1 * dz) * F(2, c) - (cSH_C1 * dx) * F(3, c);
+        if (deg > 1) {
+            const float xx = dx * dx, yy = dy * dy, zz = dz * dz, xy = dx * dy, yz = dy * dz, zx = dz * dx;
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                res[c] = res[c] + (cSH_C2[0] * xy) * F(4, c) + (cSH_C2[1] * yz) * F(5, c) +
+                         (cSH_C2[2] * (2.0f * zz - xx - yy)) * F(6, c) + (cSH_C2[3] * zx) * F(7, c) +
+                         (cSH_C2[4] * (xx - yy)) * F(8, c);
+            if (deg > 2) {
+                const float s12 = (cSH_C3[3] * dz) * (2.0f * zz - 3.0f * xx - 3.0f * yy);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float r = res[c] + ((cSH_C3[0] * dy) * (3.0f * xx - yy)) * F(9, c) +
+                              ((cSH_C3[1] * xy) * dz) * F(10, c) +
+                              ((cSH_C3[2] * dy) * (4.0f * zz - xx - yy)) * F(11, c);
+                    if (compat) r = r + s12 + F(12, c);  // common.slang:69 as written
+                    else r = r + s12 * F(12, c);
+                    r = r + ((cSH_C3[4] * dx) * (4.0f * zz - xx - yy)) * F(13, c) +
+                        ((cSH_C3[5] * dz) * (xx - yy)) * F(14, c) + ((cSH_C3[6] * dx) * (xx - 3.0f * yy)) * F(15, c);
+                    res[c] = r;
+                }
+            }
+        }
+    }
+
+    s.r = fmaxf(res[0] + 0.5f, 0.0f);
+    s.g = fmaxf(res[1] + 0.5f, 0.0f);
+    s.b = fmaxf(res[2] + 0.5f, 0.0f);
+    s.tiles = touched;
+    s.px = px;
+    s.py = py;
+    s.depth = vp[2];
+    s.radius = radius;
+    s.cx = conic0;
+    s.cy = conic1;
+    s.cz = conic2;
+    s.opacity = pos_op.w;
+    return touched;
+}
+
+// Dynamic shared memory: records (30,720 B), then per-(view, thread) tile counts.
+__global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* srec = reinterpret_cast<float*>(smem_raw);
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(smem_raw + kPreThreads * kRecordBytes);  // [n_views][128]
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t s_part;
+    __shared__ uint32_t s_wsum[kMaxViews][kPreThreads / 32];
+    __shared__ uint32_t s_excl;
+
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        s_part = atomicAdd(&a.ctl->ticket[kTicketPreprocess], 1u);
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const uint32_t part = s_part;
+    const uint32_t base = part * kPreThreads;
+    const uint32_t cnt = min(kPreThreads, a.n - base);
+    if (tid == 0) {
+        const uint32_t bytes = cnt * kRecordBytes;  // multiple of 16 (240 = 15 x 16)
+        mbar_arrive_expect_tx(&bar, bytes);
+        bulk_copy_g2s(srec, a.recs + size_t(base) * kRecordFloats, bytes, &bar);
+    }
+    const bool staged = mbar_wait_bounded(&bar, 0, &a.ctl->status);
+
+    const uint32_t i = base + tid;
+    const uint32_t e = (tid < cnt && a.ent_idx) ? a.ent_idx[i] : 0u;
+    uint32_t vis = 0;
+    for (uint32_t v = 0; v < a.n_views; ++v) {
+        uint32_t tiles = 0;
+        Splat sp;
+        if (tid < cnt && staged) {
+            const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
+            float emr[kEntityMatFloats];
+#pragma unroll
+            for (int k = 0; k < kEntityMatFloats; ++k) emr[k] = __ldg(em + k);
+            tiles = project_one(Rec{srec + tid * kRecordFloats}, emr, a.views[v], a.sh_degree, a.band3_compat != 0,
+                                sp);
+        } else {
+            sp = Splat{0.f, 0.f, 0.f, 0u, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        }
+        if (tid < cnt) {
+            float4* dst = reinterpret_cast<float4*>(a.splats + size_t(v) * a.n + i);
+            const float4* src = reinterpret_cast<const float4*>(&sp);
+            dst[0] = src[0];
+            dst[1] = src[1];
+            dst[2] = src[2];
+        }
+        s_cnt[v * kPreThreads + tid] = tiles;
+        vis += tiles > 0 ? 1u : 0u;
+    }
+    if (!a.offsets) return;
+
+    // Fused exclusive scan of tile counts (prefix.slang). The sequence is
+    // ordered (partition, view, thread): within each view, Gaussians keep
+    // index order, so keys come out in the reference's emission order.
+    const uint32_t lane = tid & 31u, warp = tid >> 5;
+    for (uint32_t v = 0; v < a.n_views; ++v) {
+        const uint32_t c = s_cnt[v * kPreThreads + tid];
+        const uint32_t incl = warp_inclusive_scan(c);
+        s_cnt[v * kPreThreads + tid] = incl - c;  // exclusive prefix inside the warp
+        if (lane == 31) s_wsum[v][warp] = incl;
+    }
+    vis = warp_sum(vis);
+    __syncthreads();
+    uint32_t total = 0;
+    for (uint32_t v = 0; v < a.n_views; ++v)
+#pragma unroll
+        for (uint32_t w = 0; w < kPreThreads / 32; ++w) total += s_wsum[v][w];
+    if (warp == 0) {
+        const uint32_t ex = warp_lookback(a.desc, part, total, a.ctl->tag * 16u + 0u, &a.ctl->status, a.spin_limit,
+                                          a.never_publish != 0);
+        if (lane == 0) {
+            s_excl = ex;
+            const uint32_t nparts = (a.n + kPreThreads - 1) / kPreThreads;
+            if (part == nparts - 1) a.ctl->total_keys = ex + total;
+        }
+    }
+    if (lane == 0 && vis) atomicAdd(&a.ctl->visible, vis);
+    __syncthreads();
+    if (tid < cnt) {
+        uint32_t run = s_excl;
+        for (uint32_t v = 0; v < a.n_views; ++v) {
+            uint32_t wb = 0, vt = 0;
+#pragma unroll
+            for (uint32_t w = 0; w < kPreThreads / 32; ++w) {
+                const uint32_t sw = s_wsum[v][w];
+                if (w < warp) wb += sw;
+                vt += sw;
+            }
+            a.offsets[size_t(v) * a.n + i] = run + wb + s_cnt[v * kPreThreads + tid];
+            run += vt;
+        }
+    }
+}
+
+// Standalone tile-count scan: 256 threads x 4 items per partition.
+constexpr uint32_t kScanThreads = 256, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_tiles_kernel(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
+                      uint32_t spin_limit, uint32_t never_publish) {
+    __shared__ uint32_t s_part, s_excl;
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_part = atomicAdd(&ctl->ticket[kTicketScan], 1u);
+    __syncthreads();
+    const uint32_t part = s_part;
+    const uint32_t base = part * kScanTile + tid * kScanItems;
+    uint32_t v[kScanItems], sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? splats[base + k].tiles : 0u;
+        sum += v[k];
+    }
+    const uint32_t incl = warp_inclusive_scan(sum);
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    uint32_t wbase = 0, total = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kScanThreads / 32; ++w) {
+        const uint32_t sw = s_warp[w];
+        if (w < warp) wbase += sw;
+        total += sw;
+    }
+    if (warp == 0) {
+        const uint32_t ex = warp_lookback(desc, part, total, ctl->tag * 16u + 0u, &ctl->status, spin_limit,
+                                          never_publish != 0);
+        if (lane == 0) {
+            s_excl = ex;
+            const uint32_t nparts = (n + kScanTile - 1) / kScanTile;
+            if (part == nparts - 1) ctl->total_keys = ex + total;
+        }
+    }
+    __syncthreads();
+    uint32_t run = s_excl + wbase + incl - sum;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        if (base + k < n) offsets[base + k] = run;
+        run += v[k];
+    }
+}
+
+// Raw parameters -> records (activation as in GaussianGeometry.cpp:112-115:
+// sigmoid opacity, exp scale, modifier 1; the quaternion is copied as given).
+__global__ void pack_records_kernel(const float* means, const float* log_scales, const float* quats,
+                                    const float* logits, const float* sh, uint32_t n, float* recs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float* r = recs + size_t(i) * kRecordFloats;
+    r[0] = means[i * 3 + 0];
+    r[1] = means[i * 3 + 1];
+    r[2] = means[i * 3 + 2];
+    r[3] = 1.0f / (1.0f + expf(-logits[i]));
+    for (int k = 0; k < 4; ++k) r[4 + k] = quats[i * 4 + k];
+    for (int k = 0; k < 3; ++k) r[8 + k] = expf(log_scales[i * 3 + k]);
+    r[11] = 1.0f;
+    for (int k = 0; k < 48; ++k) r[12 + k] = sh[size_t(i) * 48 + k];
+}
+
+}  // namespace
+
+void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, const ViewConst* views,
+                        uint32_t n_views, float* ent_mats, cudaStream_t s) {
+    frame_begin_kernel<<<1, 256, 0, s>>>(ctl, transforms, n_ent, views, n_views, ent_mats);
+}
+
+void launch_preprocess(const PreprocessArgs& a, cudaStream_t s) {
+    if (a.n == 0 || a.n_views == 0) return;
+    const uint32_t blocks = (a.n + kPreThreads - 1) / kPreThreads;
+    const size_t smem = size_t(kPreThreads) * kRecordBytes + size_t(a.n_views) * kPreThreads * 4;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaFuncSetAttribute(preprocess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        configured = smem;
+    }
+    preprocess_kernel<<<blocks, kPreThreads, smem, s>>>(a);
+}
+
+void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
+                       uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
+    if (n == 0) return;
+    const uint32_t blocks = (n + kScanTile - 1) / kScanTile;
+    scan_tiles_kernel<<<blocks, kScanThreads, 0, s>>>(splats, n, offsets, desc, ctl, spin_limit, never_publish);
+}
+
+void launch_pack_records(const float* means, const float* log_scales, const float* quats, const float* logits,
+                         const float* sh, uint32_t n, float* recs, cudaStream_t s) {
+    if (n == 0) return;
+    pack_records_kernel<<<(n + 255) / 256, 256, 0, s>>>(means, log_scales, quats, logits, sh, n, recs);
+}
+
+}  // namespace tpd

@@ -1,0 +1,360 @@
+// sort.cu — kernel (c): stable LSD radix sort of (u64 key, u32 value) pairs.
+//
+// Reference: the 4-way (2-bit digit) LSD sort of radix-shuffle.slang:39-151,
+// radix-prefixA.slang:39-170, radix-prefixB.slang:39-169 and
+// radix-mapping.slang:40-117, driven by GaussianEngine.cpp:820-841 with
+// P = ceil((msb(tiles) + 32) / 2) passes (GaussianEngine.cpp:351-357): four
+// dispatches per pass, 21-24 passes per frame.
+//
+// GB300 form (onesweep): 8-bit digits, so a 45-bit (tile | depth) key takes 6
+// passes instead of 23.
+//  1. sort_histogram_kernel reads every key once, staging 16 KB chunks into
+//     shared memory with TMA bulk copies (double buffered), and builds the
+//     digit histograms of all passes at once (warp match-any aggregation into
+//     shared memory, one global atomic per bin per CTA).
+//  2. onesweep_kernel, once per pass: a persistent CTA takes 4096-key
+//     partitions by atomic ticket, stages keys and values with TMA, ranks keys
+//     per warp (match-any, stable within the warp-striped order), combines
+//     warps per digit, resolves each digit's global prefix by a decoupled
+//     look-back over predecessor partitions (one thread per digit, bounded
+//     spin), reorders the partition in shared memory and writes digit runs
+//     out coalesced.
+// The result is the stable sort of the pairs by the low key_bits bits, the
+// same permutation as the reference's sort.
+#include <algorithm>
+
+#include "tpd_common.cuh"
+#include "tpd_kernels.h"
+#include "tpd_scan.cuh"
+
+namespace tpd {
+namespace {
+
+constexpr uint32_t kRadixBits = 8;
+constexpr uint32_t kRadix = 1u << kRadixBits;
+constexpr uint32_t kSortThreads = 256;
+constexpr uint32_t kSortWarps = kSortThreads / 32;
+constexpr uint32_t kSortItems = 16;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // 4096 keys per partition
+constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K
+
+constexpr uint32_t kHistThreads = 256;
+constexpr uint32_t kHistChunk = 2048;  // keys per TMA chunk (16 KB)
+
+struct OnesweepSmem {
+    uint64_t keys[kSortTile];
+    uint32_t vals[kSortTile];
+    uint32_t whist[kSortWarps][kRadix];
+    uint32_t gdig[kRadix];    // global exclusive digit offsets of this pass
+    uint32_t lstart[kRadix];  // block-local digit start
+    uint32_t gmap[kRadix];    // global position of local index 0 of each digit
+    uint32_t wsum[kSortWarps];
+    uint64_t bar;
+    uint32_t part;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Block-wide exclusive scan of one value per thread (256 threads); returns the exclusive prefix.
+__device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t* wsum) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t incl = warp_inclusive_scan(v);
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kSortWarps; ++w)
+        if (w < warp) base += wsum[w];
+    __syncthreads();
+    return base + incl - v;
+}
+
+__global__ void sort_begin_kernel(FrameCtl* ctl, uint32_t total) {
+    const uint32_t t = threadIdx.x;
+    for (uint32_t i = t; i < 16; i += blockDim.x) ctl->ticket[i] = 0;
+    for (uint32_t i = t; i < 8 * 256; i += blockDim.x) (&ctl->sort_hist[0][0])[i] = 0;
+    if (t == 0) {
+        ctl->tag = ctl->tag + 1;
+        ctl->status = 0;
+        ctl->total_keys = total;
+    }
+}
+
+__device__ __forceinline__ void hist_add(uint32_t* h, uint32_t d) {
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    const uint32_t leader = __ffs(peers) - 1;
+    if ((threadIdx.x & 31u) == leader && d < kRadix) atomicAdd(&h[d], __popc(peers));
+}
+
+__global__ void __launch_bounds__(kHistThreads)
+    sort_histogram_kernel(const uint64_t* __restrict__ keys, uint32_t capacity, uint32_t passes, uint32_t key_bits,
+                          FrameCtl* ctl) {
+    __shared__ uint32_t sh[8][kRadix];
+    __shared__ __align__(128) uint64_t stage[2][kHistChunk];
+    __shared__ __align__(8) uint64_t bar[2];
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t i = tid; i < 8 * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(ctl->total_keys, capacity);
+    const uint32_t nfull = K / kHistChunk;  // full chunks go through TMA
+    uint32_t shift[8], mask[8];
+#pragma unroll
+    for (uint32_t p = 0; p < 8; ++p) {
+        shift[p] = p * kRadixBits;
+        const uint32_t b = (p * kRadixBits < key_bits) ? min(kRadixBits, key_bits - p * kRadixBits) : 0u;
+        mask[p] = (1u << b) - 1u;
+    }
+    auto issue = [&](uint32_t c, uint32_t st) {
+        mbar_arrive_expect_tx(&bar[st], kHistChunk * 8);
+        bulk_copy_g2s(stage[st], keys + size_t(c) * kHistChunk, kHistChunk * 8, &bar[st]);
+    };
+    uint32_t c = blockIdx.x;
+    if (tid == 0) {
+        if (c < nfull) issue(c, 0);
+        if (c + gridDim.x < nfull) issue(c + gridDim.x, 1);
+    }
+    uint32_t phase[2] = {0, 0};
+    uint32_t it = 0;
+    for (; c < nfull; c += gridDim.x, ++it) {
+        const uint32_t st = it & 1u;
+        const bool ok = mbar_wait_bounded(&bar[st], phase[st], &ctl->status);
+        phase[st] ^= 1u;
+        if (ok) {
+#pragma unroll 2
+            for (uint32_t j = tid; j < kHistChunk; j += kHistThreads) {
+                const uint64_t k = stage[st][j];
+                for (uint32_t p = 0; p < passes; ++p) hist_add(sh[p], uint32_t(k >> shift[p]) & mask[p]);
+            }
+        }
+        fence_proxy_async_smem();
+        __syncthreads();  // stage[st] free again
+        if (tid == 0 && c + 2 * gridDim.x < nfull) issue(c + 2 * gridDim.x, st);
+    }
+    // tail keys (fewer than one chunk) with plain loads, by CTA 0
+    if (blockIdx.x == 0) {
+        const uint32_t tail0 = nfull * kHistChunk;
+        const uint32_t tail_end = tail0 + (K - tail0 + kHistThreads - 1) / kHistThreads * kHistThreads;
+        for (uint32_t j = tail0 + tid; j < tail_end; j += kHistThreads) {  // uniform trip count
+            const bool v = j < K;
+            const uint64_t k = v ? keys[j] : 0ull;
+            for (uint32_t p = 0; p < passes; ++p)
+                hist_add(sh[p], v ? (uint32_t(k >> shift[p]) & mask[p]) : kInvalidDigit);
+        }
+    }
+    __syncthreads();
+    for (uint32_t p = 0; p < passes; ++p)
+        for (uint32_t d = tid; d < kRadix; d += kHistThreads)
+            if (sh[p][d]) atomicAdd(&ctl->sort_hist[p][d], sh[p][d]);
+}
+
+__global__ void __launch_bounds__(kSortThreads, 2)
+    onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                    uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
+                    uint32_t pass, uint32_t shift, uint32_t bits, uint64_t* __restrict__ desc, FrameCtl* ctl,
+                    uint32_t spin_limit) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    OnesweepSmem& S = *reinterpret_cast<OnesweepSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(ctl->total_keys, capacity);
+    const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
+    const uint32_t tag = ctl->tag * 16u + 1u + pass;
+    const uint32_t mask = (1u << bits) - 1u;
+
+    // global exclusive digit offsets (histogram of this pass, scanned)
+    {
+        const uint32_t h = ctl->sort_hist[pass][tid];
+        const uint32_t ex = block_exclusive_scan256(h, S.wsum);
+        S.gdig[tid] = ex;
+    }
+    if (tid == 0) {
+        mbar_init(&S.bar, 1);
+        fence_mbar_init();
+    }
+    uint32_t phase = 0;
+
+    while (true) {
+        fence_proxy_async_smem();
+        if (tid == 0) S.part = atomicAdd(&ctl->ticket[kTicketSortBase + pass], 1u);
+#pragma unroll
+        for (uint32_t w = 0; w < kSortWarps; ++w) S.whist[w][tid] = 0;
+        __syncthreads();
+        const uint32_t part = S.part;
+        if (part >= nparts) break;
+        const uint32_t base = part * kSortTile;
+        const uint32_t cnt = min(kSortTile, K - base);
+
+        // stage the partition
+        bool staged = true;
+        if (cnt == kSortTile) {
+            if (tid == 0) {
+                mbar_arrive_expect_tx(&S.bar, kSortTile * 12);
+                bulk_copy_g2s(S.keys, keys_in + base, kSortTile * 8, &S.bar);
+                bulk_copy_g2s(S.vals, vals_in + base, kSortTile * 4, &S.bar);
+            }
+            staged = mbar_wait_bounded(&S.bar, phase, &ctl->status);
+            phase ^= 1u;
+            staged = __syncthreads_and(staged) != 0;
+        } else {
+            for (uint32_t j = tid; j < cnt; j += kSortThreads) {
+                S.keys[j] = keys_in[base + j];
+                S.vals[j] = vals_in[base + j];
+            }
+            __syncthreads();
+        }
+
+        // warp-striped items: warp w owns [w*512, w*512+512), item i covers 32 consecutive keys
+        // dr[i] packs the digit (bits 0..8, kInvalidDigit for keys past K) and the
+        // rank of the key among equal digits earlier in the warp (bits 9..31)
+        uint64_t k[kSortItems];
+        uint32_t v[kSortItems], dr[kSortItems];
+#pragma unroll
+        for (uint32_t i = 0; i < kSortItems; ++i) {
+            const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
+            const bool valid = idx < cnt && staged;
+            k[i] = valid ? S.keys[idx] : ~0ull;
+            v[i] = valid ? S.vals[idx] : 0u;
+            dr[i] = valid ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
+        }
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (uint32_t i = 0; i < kSortItems; ++i) {
+            const uint32_t d = dr[i];
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+            const uint32_t leader = __ffs(peers) - 1;
+            uint32_t prev = 0;
+            if (lane == leader && d < kRadix) {
+                prev = S.whist[warp][d];
+                S.whist[warp][d] = prev + __popc(peers);
+            }
+            prev = __shfl_sync(0xFFFFFFFFu, prev, leader);
+            dr[i] = d | ((prev + __popc(peers & lt)) << 9);
+            __syncwarp();
+        }
+        __syncthreads();
+
+        // per digit (thread = digit): warp prefixes, block count, local start
+        uint32_t count = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kSortWarps; ++w) {
+            const uint32_t c = S.whist[w][tid];
+            S.whist[w][tid] = count;
+            count += c;
+        }
+        const uint32_t lstart = block_exclusive_scan256(count, S.wsum);
+
+        // decoupled look-back for this digit
+        uint64_t* dp = desc + size_t(part) * kRadix + tid;
+        st_relaxed_u64(dp, make_desc(part == 0 ? kFlagPrefix : kFlagAggregate, tag, count));
+        uint32_t excl = 0;
+        if (part > 0) {
+            int64_t p = int64_t(part) - 1;
+            uint32_t spins = 0;
+            while (p >= 0) {
+                const uint64_t d = ld_relaxed_u64(desc + size_t(p) * kRadix + tid);
+                const uint32_t f = desc_flag(d, tag);
+                if (f == 0u) {
+                    if (++spins > spin_limit) {
+                        atomicOr(&ctl->status, kStatusLookbackTimeout);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                excl += uint32_t(d);
+                if (f == uint32_t(kFlagPrefix)) break;
+                --p;
+            }
+            st_relaxed_u64(dp, make_desc(kFlagPrefix, tag, excl + count));
+        }
+        S.lstart[tid] = lstart;
+        S.gmap[tid] = S.gdig[tid] + excl - lstart;
+        __syncthreads();
+
+        // reorder the partition in shared memory (stable: warp order, then item, then lane)
+#pragma unroll
+        for (uint32_t i = 0; i < kSortItems; ++i) {
+            const uint32_t d = dr[i] & 511u;
+            if (d < kRadix) {
+                const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                S.keys[pos] = k[i];
+                S.vals[pos] = v[i];
+            }
+        }
+        __syncthreads();
+
+        // coalesced write-out of digit runs
+        if (staged) {
+            for (uint32_t j = tid; j < cnt; j += kSortThreads) {
+                const uint64_t key = S.keys[j];
+                const uint32_t d = uint32_t(key >> shift) & mask;
+                const uint32_t g = S.gmap[d] + j;
+                if (g < capacity) {
+                    keys_out[g] = key;
+                    vals_out[g] = S.vals[j];
+                }
+            }
+        }
+    }
+}
+
+int g_onesweep_blocks_per_sm = 0;
+
+}  // namespace
+
+uint32_t sort_pass_count(uint32_t key_bits) { return (key_bits + kRadixBits - 1) / kRadixBits; }
+
+size_t sort_desc_entries(uint32_t capacity) {
+    return (size_t(capacity) + kSortTile - 1) / kSortTile * kRadix + kRadix;
+}
+
+void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s) { sort_begin_kernel<<<1, 256, 0, s>>>(ctl, total); }
+
+bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
+                 uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 cudaStream_t s, cudaEvent_t after_hist) {
+    const uint32_t passes = sort_pass_count(key_bits);
+    if (passes == 0 || capacity == 0) return false;
+    const int sms = num_sms > 0 ? num_sms : 148;
+    const uint32_t max_parts = (capacity + kSortTile - 1) / kSortTile;
+    {
+        const uint32_t hist_blocks = std::max(1u, std::min<uint32_t>(uint32_t(sms) * 4u, capacity / kHistChunk + 1u));
+        sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, passes, key_bits, ctl);
+    }
+    if (after_hist) cudaEventRecord(after_hist, s);
+    const size_t smem = sizeof(OnesweepSmem);
+    if (g_onesweep_blocks_per_sm == 0) {
+        cudaFuncSetAttribute(onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, onesweep_kernel, kSortThreads, smem);
+        g_onesweep_blocks_per_sm = b > 0 ? b : 1;
+    }
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * g_onesweep_blocks_per_sm)));
+    uint64_t* kin = keys;
+    uint32_t* vin = vals;
+    uint64_t* kout = keys_alt;
+    uint32_t* vout = vals_alt;
+    for (uint32_t p = 0; p < passes; ++p) {
+        const uint32_t shift = p * kRadixBits;
+        const uint32_t bits = std::min(kRadixBits, key_bits - shift);
+        onesweep_kernel<<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc, ctl,
+                                                         spin_limit);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    return (passes & 1u) != 0;
+}
+
+}  // namespace tpd
