@@ -92,7 +92,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
 // Bounded wait on an mbarrier phase. Returns false (and sets the status bit)
 // when the limit runs out; the caller then skips the staged data.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, uint32_t* status,
-                                                  uint32_t limit = (1u << 24)) {
+                                                  uint32_t limit = (1u << 20)) {
     for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, phase)) return true;
     atomicOr(status, kStatusMbarTimeout);
