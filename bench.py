@@ -186,7 +186,9 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the engine launches on it and the timing events are recorded on it
+    stream = torch.cuda.Stream(dev)
+    assert stream.cuda_stream != 0
 
     cfg = configs.CONFIGS[args.config]
     sc = configs.scene(cfg)
