@@ -29,17 +29,51 @@ constexpr float kAlphaMin = 1.0f / 255.0f;
 constexpr float kAlphaMax = 0.99f;
 constexpr float kTMin = 0.0001f;
 
-struct PairEval {
-    float dx, dy, G, alpha, raw_alpha;
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLn2 = 0.6931471805599453f;
+
+// A list entry staged in shared memory. The conic is pre-scaled so that
+//   p2 = log2(e) * power,  power = -0.5 * (cx*dx*dx + cz*dy*dy) - cy*dx*dy  (blend.slang:83-84)
+// costs five multiply/fma operations, exp(power) = 2^p2 is one ex2, and
+//   alpha = min(0.99, o * 2^p2) < 1/255  <=>  p2 < thr = log2(1 / (255 o))
+// is decided before the exponential. Forward and adjoint stage and test
+// entries with the same functions, so they take identical decisions.
+struct Staged {
+    float2 xy;   // px, py
+    float4 q;    // qa = -0.5 log2e cx, qb = -log2e cy, qc = -0.5 log2e cz, thr
+    float4 col;  // r, g, b, opacity
 };
 
-// -0.5 * (cx*dx*dx + cz*dy*dy) - cy*dx*dy with d = xy - pixel (blend.slang:83-84).
-__device__ __forceinline__ float pair_power(float2 xy, float4 co, float pxf, float pyf, float& dx, float& dy) {
+__device__ __forceinline__ void stage_entry(const Splat* sp, float2& xy, float4& q, float4& col) {
+    const float4* p = reinterpret_cast<const float4*>(sp);
+    const float4 c = __ldg(p + 0), tex = __ldg(p + 1), co = __ldg(p + 2);
+    xy = make_float2(tex.x, tex.y);
+    const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : __int_as_float(0x7f800000);  // +inf: never blends
+    q = make_float4(-0.5f * kLog2e * co.x, -kLog2e * co.y, -0.5f * kLog2e * co.z, thr);
+    col = make_float4(c.x, c.y, c.z, co.w);
+}
+
+__device__ __forceinline__ void stage_empty(float2& xy, float4& q, float4& col) {
+    xy = make_float2(0.f, 0.f);
+    q = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7f800000));
+    col = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ float pair_p2(float2 xy, float4 q, float pxf, float pyf, float& dx, float& dy) {
     dx = __fsub_rn(xy.x, pxf);
     dy = __fsub_rn(xy.y, pyf);
-    const float q = __fmaf_rn(__fmul_rn(co.x, dx), dx, __fmul_rn(__fmul_rn(co.z, dy), dy));
-    return __fmaf_rn(-0.5f, q, -__fmul_rn(__fmul_rn(co.y, dx), dy));
+    const float t = __fmaf_rn(q.y, dy, __fmul_rn(q.x, dx));
+    return __fmaf_rn(t, dx, __fmul_rn(__fmul_rn(q.z, dy), dy));
 }
+
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// true when the pair is skipped (power > 0 or alpha < 1/255)
+__device__ __forceinline__ bool pair_skipped(float p2, float thr) { return p2 > 0.0f || p2 < thr; }
 
 __device__ __forceinline__ void load_view_tile(const BlendArgs* /*unused*/, const ViewConst* views,
                                                const uint32_t* tile_view, uint32_t tile, uint32_t& vi,
@@ -56,7 +90,7 @@ __device__ __forceinline__ void load_view_tile(const BlendArgs* /*unused*/, cons
 
 __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     __shared__ float2 s_xy[kBlendThreads];
-    __shared__ float4 s_co[kBlendThreads];
+    __shared__ float4 s_q[kBlendThreads];
     __shared__ float4 s_col[kBlendThreads];
 
     const uint32_t tile = blockIdx.x;
@@ -79,34 +113,25 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
         const uint32_t j = b0 + tid;
         if (j < end) {
             const uint32_t idx = a.vals[j];
-            if (idx < a.n) {
-                const float4* sp = reinterpret_cast<const float4*>(vsplats + idx);
-                const float4 col = __ldg(sp + 0), tex = __ldg(sp + 1), co = __ldg(sp + 2);
-                s_xy[tid] = make_float2(tex.x, tex.y);
-                s_co[tid] = co;
-                s_col[tid] = col;
-            } else {  // only reachable with corrupted lists: an entry that never contributes
-                s_xy[tid] = make_float2(0.f, 0.f);
-                s_co[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
-                s_col[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
+            if (idx < a.n) stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid]);
+            else stage_empty(s_xy[tid], s_q[tid], s_col[tid]);  // only reachable with corrupted lists
         }
         __syncthreads();
         const uint32_t n = min(kBlendThreads, end - b0);
         if (!done) {
+#pragma unroll 4
             for (uint32_t jj = 0; jj < n; ++jj) {
                 float dx, dy;
-                const float4 co = s_co[jj];
-                const float power = pair_power(s_xy[jj], co, pxf, pyf, dx, dy);
-                if (power > 0.0f) continue;
-                const float alpha = fminf(kAlphaMax, __fmul_rn(co.w, __expf(power)));
-                if (alpha < kAlphaMin) continue;
+                const float4 q = s_q[jj];
+                const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
+                if (pair_skipped(p2, q.w)) continue;
+                const float4 col = s_col[jj];
+                const float alpha = fminf(kAlphaMax, __fmul_rn(col.w, ex2_approx(p2)));
                 const float tn = __fmul_rn(T, __fsub_rn(1.0f, alpha));
                 if (tn < kTMin) {
                     done = true;
                     break;
                 }
-                const float4 col = s_col[jj];
                 const float w = __fmul_rn(alpha, T);
                 C0 = __fmaf_rn(col.x, w, C0);
                 C1 = __fmaf_rn(col.y, w, C1);
@@ -149,7 +174,7 @@ constexpr int kG2D = 9;  // px, py, conic.x, conic.y, conic.z, opacity, r, g, b
 
 __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBackwardArgs a) {
     __shared__ float2 s_xy[kBlendThreads];
-    __shared__ float4 s_co[kBlendThreads];
+    __shared__ float4 s_q[kBlendThreads];
     __shared__ float4 s_col[kBlendThreads];
     __shared__ uint32_t s_idx[kBlendThreads];
     __shared__ float s_acc[kBlendThreads][kG2D + 1];
@@ -197,16 +222,10 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
             const uint32_t e = uint32_t(r_end) - 1u - tid;  // descending list position (relative)
             uint32_t idx = a.vals[start + e];
             if (idx < a.n) {
-                const float4* sp = reinterpret_cast<const float4*>(vsplats + idx);
-                const float4 col = __ldg(sp + 0), tex = __ldg(sp + 1), co = __ldg(sp + 2);
-                s_xy[tid] = make_float2(tex.x, tex.y);
-                s_co[tid] = co;
-                s_col[tid] = col;
+                stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid]);
             } else {  // only reachable with corrupted lists
                 idx = 0;
-                s_xy[tid] = make_float2(0.f, 0.f);
-                s_co[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
-                s_col[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+                stage_empty(s_xy[tid], s_q[tid], s_col[tid]);
             }
             s_idx[tid] = idx;
         }
@@ -220,36 +239,35 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
             bool contrib = false;
             if (inside && e < last) {
                 float dx, dy;
-                const float4 co = s_co[jj];
-                const float power = pair_power(s_xy[jj], co, pxf, pyf, dx, dy);
-                if (power <= 0.0f) {
-                    const float G = __expf(power);
-                    const float raw = __fmul_rn(co.w, G);
+                const float4 q = s_q[jj];
+                const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
+                if (!pair_skipped(p2, q.w)) {
+                    const float4 col = s_col[jj];
+                    const float G = ex2_approx(p2);
+                    const float raw = __fmul_rn(col.w, G);
                     const float alpha = fminf(kAlphaMax, raw);
-                    if (alpha >= kAlphaMin) {
-                        contrib = true;
-                        const float one_m = 1.0f - alpha;
-                        const float Tb = T / one_m;  // transmittance in front of this entry
-                        const float4 col = s_col[jj];
-                        const float w = alpha * Tb;
-                        gv[6] = g0 * w;
-                        gv[7] = g1 * w;
-                        gv[8] = g2 * w;
-                        const float dA = g0 * (col.x * Tb - S0 / one_m) + g1 * (col.y * Tb - S1 / one_m) +
-                                         g2 * (col.z * Tb - S2 / one_m);
-                        S0 = fmaf(col.x, w, S0);
-                        S1 = fmaf(col.y, w, S1);
-                        S2 = fmaf(col.z, w, S2);
-                        T = Tb;
-                        if (raw <= kAlphaMax) {
-                            const float dpow = dA * alpha;
-                            gv[5] = dA * G;
-                            gv[0] = dpow * (-co.x * dx - co.y * dy);
-                            gv[1] = dpow * (-co.z * dy - co.y * dx);
-                            gv[2] = dpow * (-0.5f * dx * dx);
-                            gv[3] = dpow * (-dx * dy);
-                            gv[4] = dpow * (-0.5f * dy * dy);
-                        }
+                    contrib = true;
+                    const float one_m = 1.0f - alpha;
+                    const float Tb = T / one_m;  // transmittance in front of this entry
+                    const float w = alpha * Tb;
+                    gv[6] = g0 * w;
+                    gv[7] = g1 * w;
+                    gv[8] = g2 * w;
+                    const float dA = g0 * (col.x * Tb - S0 / one_m) + g1 * (col.y * Tb - S1 / one_m) +
+                                     g2 * (col.z * Tb - S2 / one_m);
+                    S0 = fmaf(col.x, w, S0);
+                    S1 = fmaf(col.y, w, S1);
+                    S2 = fmaf(col.z, w, S2);
+                    T = Tb;
+                    if (raw <= kAlphaMax) {
+                        // power = p2 ln2; d power / d(dx, dy) = ln2 (2 qa dx + qb dy, 2 qc dy + qb dx)
+                        const float dpow = dA * alpha;
+                        gv[5] = dA * G;
+                        gv[0] = dpow * kLn2 * (2.0f * q.x * dx + q.y * dy);
+                        gv[1] = dpow * kLn2 * (2.0f * q.z * dy + q.y * dx);
+                        gv[2] = dpow * (-0.5f * dx * dx);
+                        gv[3] = dpow * (-dx * dy);
+                        gv[4] = dpow * (-0.5f * dy * dy);
                     }
                 }
             }

@@ -260,11 +260,12 @@ void enqueue_frame(tpd_engine* e) {
     launch_preprocess(pa, s);
     mark(1);
     const uint32_t cap = uint32_t(e->capacity);
-    launch_keygen(e->d_splats, e->d_offsets, e->n, e->d_views, e->n_views, e->d_keys[0], e->d_vals[0], cap, e->d_ctl,
-                  s);
+    launch_keygen(e->d_splats, e->d_offsets, e->n, e->d_views, e->n_views, e->d_keys[0], e->d_vals[0], cap,
+                  e->key_bits, e->d_ctl, e->num_sms, s);
     mark(2);
     e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, e->key_bits,
-                                   e->d_desc_sort, e->d_ctl, pa.spin_limit, e->num_sms, s, ev ? ev[3] : nullptr);
+                                   e->d_desc_sort, e->d_ctl, pa.spin_limit, e->num_sms, s, ev ? ev[3] : nullptr,
+                                   /*hist_ready=*/true);
     mark(4);
     const int b = e->sorted_in_alt ? 1 : 0;
     launch_tile_ranges(e->d_keys[b], e->total_tiles, e->d_ranges, e->d_ctl, cap, e->num_sms, s);

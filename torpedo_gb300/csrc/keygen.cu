@@ -18,16 +18,33 @@ namespace {
 
 constexpr uint32_t kKeygenThreads = 256;
 
+constexpr uint32_t kNoDigit = 0x1000u;
+
+// Adds 1 per lane to sh[d] for lanes with d != kNoDigit, one atomic per distinct digit.
+__device__ __forceinline__ void warp_hist_add(uint32_t* sh, uint32_t d, uint32_t lane) {
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    if (d != kNoDigit && lane == uint32_t(__ffs(peers) - 1)) atomicAdd(&sh[d], uint32_t(__popc(peers)));
+}
+
+// Besides the keys, builds the radix sort's digit histograms of all passes
+// (ctl->sort_hist): a Gaussian's keys share their low 32 bits (depth), so the
+// depth digits are counted once per Gaussian with its tile count as weight;
+// only the tile-id digits are counted per key.
 __global__ void __launch_bounds__(kKeygenThreads)
     keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ offsets, uint32_t n,
                   const ViewConst* __restrict__ views, uint32_t n_views, uint64_t* __restrict__ keys,
-                  uint32_t* __restrict__ vals, uint32_t capacity, FrameCtl* ctl) {
+                  uint32_t* __restrict__ vals, uint32_t capacity, uint32_t key_bits, FrameCtl* ctl) {
+    __shared__ uint32_t sh[8][256];
     const uint32_t lane = lane_id();
     const uint32_t warps_total = (gridDim.x * blockDim.x) >> 5;
     const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
     const uint32_t wpv = (n + 31) / 32;  // warps per view; a warp never straddles a view or a 128-partition
     if (ctl->status & kStatusFatal) return;
+    const uint32_t npass = min(8u, (key_bits + 7) / 8);
+    for (uint32_t k = threadIdx.x; k < 8 * 256; k += blockDim.x) (&sh[0][0])[k] = 0;
+    __syncthreads();
+    auto digit_mask = [&](uint32_t p) { return (1u << min(8u, key_bits - 8 * p)) - 1u; };
 
     for (uint32_t wi = warp_global; wi < wpv * n_views; wi += warps_total) {
         const uint32_t v = wi / wpv;
@@ -47,6 +64,10 @@ __global__ void __launch_bounds__(kKeygenThreads)
         }
         const uint32_t w = x1 - x0;
         const uint32_t cnt = w * (y1 - y0);
+        if (cnt) {
+            for (uint32_t p = 0; p < min(npass, 4u); ++p)
+                atomicAdd(&sh[p][(depth_bits >> (8 * p)) & digit_mask(p)], cnt);
+        }
         const uint32_t incl = warp_inclusive_scan(cnt);
         const uint32_t excl = incl - cnt;
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
@@ -66,18 +87,27 @@ __global__ void __launch_bounds__(kKeygenThreads)
             const uint32_t jw = __shfl_sync(0xFFFFFFFFu, w, j);
             const uint32_t jex = __shfl_sync(0xFFFFFFFFu, excl, j);
             const uint32_t jdb = __shfl_sync(0xFFFFFFFFu, depth_bits, j);
-            if (s < total) {
+            uint32_t tile = 0;
+            const bool live = s < total;
+            if (live) {
                 const uint32_t local = s - jex;
                 const uint32_t ty = jy0 + local / jw;
                 const uint32_t tx = jx0 + local % jw;
+                tile = tile_base + ty * gx + tx;
                 const uint64_t pos = uint64_t(base) + s;
                 if (pos < capacity) {
-                    keys[pos] = (uint64_t(tile_base + ty * gx + tx) << 32) | uint64_t(jdb);
+                    keys[pos] = (uint64_t(tile) << 32) | uint64_t(jdb);
                     vals[pos] = g0 + j;
                 }
             }
+            for (uint32_t p = 4; p < npass; ++p)
+                warp_hist_add(sh[p], live ? ((tile >> (8 * (p - 4))) & digit_mask(p)) : kNoDigit, lane);
         }
     }
+    __syncthreads();
+    for (uint32_t p = 0; p < npass; ++p)
+        for (uint32_t d = threadIdx.x; d < 256; d += blockDim.x)
+            if (sh[p][d]) atomicAdd(&ctl->sort_hist[p][d], sh[p][d]);
 }
 
 // range.slang:18-35 over K = min(total_keys, capacity) keys; ranges zeroed first.
@@ -105,14 +135,15 @@ __global__ void tile_ranges_kernel(const uint64_t* __restrict__ keys, uint32_t* 
 }  // namespace
 
 void launch_keygen(const Splat* splats, const uint32_t* offsets, uint32_t n, const ViewConst* views,
-                   uint32_t n_views, uint64_t* keys, uint32_t* vals, uint32_t capacity, FrameCtl* ctl,
-                   cudaStream_t s) {
+                   uint32_t n_views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
+                   FrameCtl* ctl, int num_sms, cudaStream_t s) {
     if (n == 0 || n_views == 0) return;
     const uint64_t warps = uint64_t((n + 31) / 32) * n_views;
     uint64_t blocks = (warps * 32 + kKeygenThreads - 1) / kKeygenThreads;
-    blocks = blocks < 8192u ? blocks : 8192u;
+    const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * 8;  // persistent: bounded histogram flushes
+    blocks = blocks < cap ? blocks : cap;
     keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, offsets, n, views, n_views, keys, vals,
-                                                              capacity, ctl);
+                                                              capacity, key_bits, ctl);
 }
 
 void launch_tile_ranges(const uint64_t* keys, uint32_t n_tiles, uint32_t* ranges, FrameCtl* ctl, uint32_t capacity,

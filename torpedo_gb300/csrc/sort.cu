@@ -160,7 +160,45 @@ __global__ void __launch_bounds__(kHistThreads)
             if (sh[p][d]) atomicAdd(&ctl->sort_hist[p][d], sh[p][d]);
 }
 
-__global__ void __launch_bounds__(kSortThreads, 2)
+// Resolves the exclusive prefix of one digit for partition `part` by walking
+// predecessors; up to four descriptors are loaded per round trip.
+__device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ desc, uint32_t part, uint32_t digit,
+                                                   uint32_t tag, FrameCtl* ctl, uint32_t spin_limit) {
+    uint32_t excl = 0;
+    int64_t p = int64_t(part) - 1;
+    uint32_t spins = 0;
+    while (p >= 0) {
+        uint64_t d[4];
+        const int cnt = p >= 3 ? 4 : int(p) + 1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j < cnt) d[j] = ld_relaxed_u64(desc + size_t(p - j) * kRadix + digit);
+        bool stop = false, wait = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j >= cnt || stop || wait) continue;
+            const uint32_t f = desc_flag(d[j], tag);
+            if (f == 0u) {
+                wait = true;  // not yet published: retry from here
+            } else {
+                excl += uint32_t(d[j]);
+                --p;
+                if (f == uint32_t(kFlagPrefix)) stop = true;
+            }
+        }
+        if (stop) break;
+        if (wait) {
+            if (++spins > spin_limit) {
+                atomicOr(&ctl->status, kStatusLookbackTimeout);
+                break;
+            }
+            __nanosleep(32);
+        }
+    }
+    return excl;
+}
+
+__global__ void __launch_bounds__(kSortThreads, 3)
     onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
                     uint32_t pass, uint32_t shift, uint32_t bits, uint64_t* __restrict__ desc, FrameCtl* ctl,
@@ -215,23 +253,16 @@ __global__ void __launch_bounds__(kSortThreads, 2)
             __syncthreads();
         }
 
-        // warp-striped items: warp w owns [w*512, w*512+512), item i covers 32 consecutive keys
-        // dr[i] packs the digit (bits 0..8, kInvalidDigit for keys past K) and the
-        // rank of the key among equal digits earlier in the warp (bits 9..31)
-        uint64_t k[kSortItems];
-        uint32_t v[kSortItems], dr[kSortItems];
-#pragma unroll
-        for (uint32_t i = 0; i < kSortItems; ++i) {
-            const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-            const bool valid = idx < cnt && staged;
-            k[i] = valid ? S.keys[idx] : ~0ull;
-            v[i] = valid ? S.vals[idx] : 0u;
-            dr[i] = valid ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
-        }
+        // Warp-striped items: warp w owns [w*512, w*512+512), item i covers 32
+        // consecutive keys. dr[i] packs the digit (bits 0..8, kInvalidDigit for
+        // keys past K) and the key's rank among equal digits earlier in the
+        // warp (bits 9..31); keys themselves are re-read from shared memory.
+        uint32_t dr[kSortItems];
         const uint32_t lt = lanemask_lt();
 #pragma unroll
         for (uint32_t i = 0; i < kSortItems; ++i) {
-            const uint32_t d = dr[i];
+            const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
+            const uint32_t d = (idx < cnt && staged) ? (uint32_t(S.keys[idx] >> shift) & mask) : kInvalidDigit;
             const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
             const uint32_t leader = __ffs(peers) - 1;
             uint32_t prev = 0;
@@ -253,45 +284,50 @@ __global__ void __launch_bounds__(kSortThreads, 2)
             S.whist[w][tid] = count;
             count += c;
         }
-        const uint32_t lstart = block_exclusive_scan256(count, S.wsum);
-
-        // decoupled look-back for this digit
         uint64_t* dp = desc + size_t(part) * kRadix + tid;
         st_relaxed_u64(dp, make_desc(part == 0 ? kFlagPrefix : kFlagAggregate, tag, count));
-        uint32_t excl = 0;
-        if (part > 0) {
-            int64_t p = int64_t(part) - 1;
-            uint32_t spins = 0;
-            while (p >= 0) {
-                const uint64_t d = ld_relaxed_u64(desc + size_t(p) * kRadix + tid);
-                const uint32_t f = desc_flag(d, tag);
-                if (f == 0u) {
-                    if (++spins > spin_limit) {
-                        atomicOr(&ctl->status, kStatusLookbackTimeout);
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                excl += uint32_t(d);
-                if (f == uint32_t(kFlagPrefix)) break;
-                --p;
-            }
-            st_relaxed_u64(dp, make_desc(kFlagPrefix, tag, excl + count));
-        }
+        const uint32_t lstart = block_exclusive_scan256(count, S.wsum);  // (contains the barrier for whist)
         S.lstart[tid] = lstart;
-        S.gmap[tid] = S.gdig[tid] + excl - lstart;
         __syncthreads();
 
-        // reorder the partition in shared memory (stable: warp order, then item, then lane)
+        // reorder the partition in shared memory (stable: warp, then item, then
+        // lane) while predecessors publish; keys first, then values
+        {
+            uint64_t k[kSortItems];
 #pragma unroll
-        for (uint32_t i = 0; i < kSortItems; ++i) {
-            const uint32_t d = dr[i] & 511u;
-            if (d < kRadix) {
-                const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-                S.keys[pos] = k[i];
-                S.vals[pos] = v[i];
+            for (uint32_t i = 0; i < kSortItems; ++i) {
+                const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
+                k[i] = S.keys[min(idx, kSortTile - 1)];
             }
+            __syncthreads();
+#pragma unroll
+            for (uint32_t i = 0; i < kSortItems; ++i) {
+                const uint32_t d = dr[i] & 511u;
+                if (d < kRadix) S.keys[S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9)] = k[i];
+            }
+        }
+        {
+            uint32_t v[kSortItems];
+#pragma unroll
+            for (uint32_t i = 0; i < kSortItems; ++i) {
+                const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
+                v[i] = S.vals[min(idx, kSortTile - 1)];
+            }
+            __syncthreads();
+#pragma unroll
+            for (uint32_t i = 0; i < kSortItems; ++i) {
+                const uint32_t d = dr[i] & 511u;
+                if (d < kRadix) S.vals[S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9)] = v[i];
+            }
+        }
+
+        // decoupled look-back for this thread's digit
+        if (part > 0) {
+            const uint32_t excl = digit_lookback(desc, part, tid, tag, ctl, spin_limit);
+            st_relaxed_u64(dp, make_desc(kFlagPrefix, tag, excl + count));
+            S.gmap[tid] = S.gdig[tid] + excl - lstart;
+        } else {
+            S.gmap[tid] = S.gdig[tid] - lstart;
         }
         __syncthreads();
 
@@ -324,12 +360,12 @@ void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s) { sort_beg
 
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
                  uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
-                 cudaStream_t s, cudaEvent_t after_hist) {
+                 cudaStream_t s, cudaEvent_t after_hist, bool hist_ready) {
     const uint32_t passes = sort_pass_count(key_bits);
     if (passes == 0 || capacity == 0) return false;
     const int sms = num_sms > 0 ? num_sms : 148;
     const uint32_t max_parts = (capacity + kSortTile - 1) / kSortTile;
-    {
+    if (!hist_ready) {
         const uint32_t hist_blocks = std::max(1u, std::min<uint32_t>(uint32_t(sms) * 4u, capacity / kHistChunk + 1u));
         sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, passes, key_bits, ctl);
     }

@@ -62,10 +62,11 @@ void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint6
 
 // keygen.slang: keys = (tile_base + tile) << 32 | bits(viewZ), vals = Gaussian index,
 // for n_views x n (view, Gaussian) items. K is read from ctl->total_keys; keys
-// beyond capacity are dropped and flagged.
+// beyond capacity are dropped and flagged. Also accumulates the radix sort's
+// digit histograms for key_bits into ctl->sort_hist (cleared at frame start).
 void launch_keygen(const Splat* splats, const uint32_t* offsets, uint32_t n, const ViewConst* views,
-                   uint32_t n_views, uint64_t* keys, uint32_t* vals, uint32_t capacity, FrameCtl* ctl,
-                   cudaStream_t s);
+                   uint32_t n_views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
+                   FrameCtl* ctl, int num_sms, cudaStream_t s);
 
 // Onesweep LSD radix sort of (key, val) pairs on the low key_bits bits.
 // K = min(ctl->total_keys, capacity). Result in (keys, vals) if the pass count
@@ -73,10 +74,12 @@ void launch_keygen(const Splat* splats, const uint32_t* offsets, uint32_t n, con
 // desc: sort_desc_entries(capacity) descriptors.
 size_t sort_desc_entries(uint32_t capacity);
 uint32_t sort_pass_count(uint32_t key_bits);
-// after_hist (nullable): event recorded between the histogram and the first pass.
+// hist_ready: ctl->sort_hist already holds the digit histograms (keygen built
+// them), so the histogram kernel is skipped. after_hist (nullable): event
+// recorded between the histogram and the first pass.
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
                  uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
-                 cudaStream_t s, cudaEvent_t after_hist = nullptr);
+                 cudaStream_t s, cudaEvent_t after_hist = nullptr, bool hist_ready = false);
 // Clears status, sort histograms and tickets, sets total_keys and advances the
 // tag (standalone stage calls).
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s);
