@@ -194,7 +194,7 @@ def run_ours(args):
     sc = configs.scene(cfg)
     cam = configs.cameras(cfg)[0]
 
-    eng = T.GaussianEngine(device=local, stream=stream.cuda_stream)
+    eng = T.GaussianEngine(device=local, stream=stream.cuda_stream, sort_ctas_per_sm=args.sort_ctas)
     eng.compile(sc.records)
     eng.set_camera(cam)
     st = eng.raster_frame()
@@ -233,7 +233,8 @@ def run_ours(args):
     value = world * args.steps / (ms / 1000.0)
 
     # stage-timed region: live per-stage durations for the roofline
-    eng_t = T.GaussianEngine(device=local, stream=stream.cuda_stream, stage_timing=True)
+    eng_t = T.GaussianEngine(device=local, stream=stream.cuda_stream, stage_timing=True,
+                             sort_ctas_per_sm=args.sort_ctas)
     eng_t.compile(sc.records)
     eng_t.set_camera(cam)
     eng_t.raster_frame()
@@ -319,6 +320,7 @@ def main():
     ap.add_argument("--config", default="cfg1")
     ap.add_argument("--cpu-baseline-s", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--sort-ctas", type=int, default=2, help="radix pass kernel residency (2 or 3 CTAs per SM)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -29,7 +29,8 @@ class Settings(C.Structure):
         ("timeout_s", C.c_double),
         ("test_never_publish", C.c_uint32),
         ("stage_timing", C.c_uint32),
-        ("reserved", C.c_uint32 * 6),
+        ("sort_ctas_per_sm", C.c_uint32),
+        ("reserved", C.c_uint32 * 5),
     ]
 
 

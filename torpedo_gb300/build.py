@@ -63,7 +63,15 @@ def _compile(src: str, flags: list[str], hdr_mtime: float, verbose: bool) -> Pat
 
 
 def build(verbose: bool = False, force: bool = False) -> Path:
+    """TPD_CHECKED=1 in the environment adds -DTPD_CHECKED (extra debug checks)."""
     OUT.mkdir(exist_ok=True)
+    flags = "checked" if os.environ.get("TPD_CHECKED") == "1" else "release"
+    stamp = OUT / "flavour"
+    if not stamp.exists() or stamp.read_text() != flags:
+        force = True
+        stamp.write_text(flags)
+    if flags == "checked":
+        COMMON.append("-DTPD_CHECKED")
     if force:
         for o in OUT.glob("*.o"):
             o.unlink()

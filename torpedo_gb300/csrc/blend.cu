@@ -111,13 +111,14 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     for (uint32_t b0 = start; b0 < end; b0 += kBlendThreads) {
         if (__syncthreads_count(done) == kBlendThreads) break;
         const uint32_t j = b0 + tid;
-        if (j < end) {
+        if (j < end && TPD_INBOUNDS(a.ctl, 40, j, a.capacity)) {
             const uint32_t idx = a.vals[j];
-            if (idx < a.n) stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid]);
+            if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n)) stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid]);
             else stage_empty(s_xy[tid], s_q[tid], s_col[tid]);  // only reachable with corrupted lists
         }
         __syncthreads();
         const uint32_t n = min(kBlendThreads, end - b0);
+        if (!TPD_INBOUNDS(a.ctl, 43, n, kBlendThreads + 1)) break;
         if (!done) {
 #pragma unroll 4
             for (uint32_t jj = 0; jj < n; ++jj) {
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
             }
         }
     }
-    if (inside) {
+    if (inside && TPD_INBOUNDS(a.ctl, 41, tile, a.n_tiles)) {
         const size_t p = (a.image_offset ? a.image_offset[vi] : 0ull) + size_t(pyl) * W + pxl;
         a.image[p * 3 + 0] = C0;
         a.image[p * 3 + 1] = C1;

@@ -17,6 +17,7 @@
 //    (tile ids without offset).
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -197,7 +198,9 @@ int wait_stream(tpd_engine* e) {
     while (true) {
         const cudaError_t q = cudaEventQuery(e->done_event);
         if (q == cudaSuccess) return TPD_OK;
-        if (q != cudaErrorNotReady) return fail(e, TPD_ERR_DEVICE, std::string("frame: ") + cudaGetErrorString(q));
+        if (q != cudaErrorNotReady)
+            return fail(e, TPD_ERR_DEVICE, std::string("frame: ") + cudaGetErrorString(q) +
+                                               (e->last_error.rfind("stage", 0) == 0 ? " (" + e->last_error + ")" : ""));
         const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (dt > limit) return fail(e, TPD_ERR_TIMEOUT, "frame did not finish within the host wait limit");
         std::this_thread::sleep_for(std::chrono::microseconds(dt < 0.01 ? 20 : 500));
@@ -232,8 +235,22 @@ void enqueue_frame(tpd_engine* e) {
         ev = e->tev[slot];
         e->tev_pending[slot] = true;
     }
+    // TPD_DEBUG_SYNC=1 (eager frames only): synchronise after each stage and
+    // name the first stage whose kernels report an error.
+    static const bool debug_sync = [] {
+        const char* v = std::getenv("TPD_DEBUG_SYNC");
+        return v && v[0] == '1';
+    }();
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cap_status);
+    static const char* kStageNames[] = {"begin", "preprocess", "keygen", "sort", "sort", "ranges", "blend"};
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], s);
+        if (debug_sync && cap_status == cudaStreamCaptureStatusNone) {
+            const cudaError_t err = cudaStreamSynchronize(s);
+            if (err != cudaSuccess && e->last_error.rfind("stage", 0) != 0)
+                e->last_error = std::string("stage ") + kStageNames[k] + ": " + cudaGetErrorString(err);
+        }
     };
     mark(0);
     cudaMemcpyAsync(e->d_views, e->h_views, sizeof(ViewConst) * e->n_views, cudaMemcpyHostToDevice, s);
@@ -265,7 +282,7 @@ void enqueue_frame(tpd_engine* e) {
     mark(2);
     e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, e->key_bits,
                                    e->d_desc_sort, e->d_ctl, pa.spin_limit, e->num_sms, s, ev ? ev[3] : nullptr,
-                                   /*hist_ready=*/true);
+                                   /*hist_ready=*/true, int(e->settings.sort_ctas_per_sm));
     mark(4);
     const int b = e->sorted_in_alt ? 1 : 0;
     launch_tile_ranges(e->d_keys[b], e->total_tiles, e->d_ranges, e->d_ctl, cap, e->num_sms, s);
@@ -600,6 +617,13 @@ int tpd_raster_frame(tpd_engine* e, tpd_frame_stats* stats) {
             if (rc != TPD_OK) return rc;
             ++retries;
             continue;
+        }
+        if (h.status & kStatusBadIndex) {
+            uint32_t dbg[4] = {0, 0, 0, 0};
+            cudaMemcpy(dbg, e->d_ctl->debug, sizeof(dbg), cudaMemcpyDeviceToHost);
+            return fail(e, TPD_ERR_DEVICE, "bounds check failed: site " + std::to_string(dbg[0]) + " index " +
+                                               std::to_string((uint64_t(dbg[3]) << 32) | dbg[1]) + " bound " +
+                                               std::to_string(dbg[2]));
         }
         if (h.status & (kStatusLookbackTimeout | kStatusMbarTimeout)) {
             e->frames++;

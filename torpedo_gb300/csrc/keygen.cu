@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
         const size_t vbase = size_t(v) * n;
         const uint32_t i = g0 + lane;
         uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0, off = 0, depth_bits = 0;
-        if (i < n) {
+        if (i < n && TPD_INBOUNDS(ctl, 21, vbase + i, uint64_t(n) * n_views)) {
             const float4 texel = reinterpret_cast<const float4*>(splats + vbase + i)[1];  // px, py, viewZ, radius
             off = offsets[vbase + i];
             if (texel.w > 0.0f) {
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
                 const uint32_t tx = jx0 + local % jw;
                 tile = tile_base + ty * gx + tx;
                 const uint64_t pos = uint64_t(base) + s;
-                if (pos < capacity) {
+                if (pos < capacity && TPD_INBOUNDS(ctl, 20, g0 + j, n)) {
                     keys[pos] = (uint64_t(tile) << 32) | uint64_t(jdb);
                     vals[pos] = g0 + j;
                 }
@@ -112,18 +112,19 @@ __global__ void __launch_bounds__(kKeygenThreads)
 
 // range.slang:18-35 over K = min(total_keys, capacity) keys; ranges zeroed first.
 __global__ void tile_ranges_kernel(const uint64_t* __restrict__ keys, uint32_t* __restrict__ ranges,
-                                   uint32_t n_tiles, const FrameCtl* ctl, uint32_t capacity) {
+                                   uint32_t n_tiles, FrameCtl* ctl, uint32_t capacity) {
     if (ctl->status & kStatusFatal) return;
     const uint32_t K = min(ctl->total_keys, capacity);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < K; idx += stride) {
+        if (!TPD_INBOUNDS(ctl, 30, idx, capacity)) continue;
         const uint32_t cur = uint32_t(keys[idx] >> 32);
         if (cur >= n_tiles) continue;  // only reachable with corrupted keys
         if (idx == 0) {
             ranges[cur * 2 + 0] = 0;
         } else {
             const uint32_t prev = uint32_t(keys[idx - 1] >> 32);
-            if (cur != prev) {
+            if (cur != prev && TPD_INBOUNDS(ctl, 31, cur, n_tiles)) {
                 if (prev < n_tiles) ranges[prev * 2 + 1] = idx;
                 ranges[cur * 2 + 0] = idx;
             }

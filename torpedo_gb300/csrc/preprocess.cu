@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
     for (uint32_t v = 0; v < a.n_views; ++v)
 #pragma unroll
         for (uint32_t w = 0; w < kPreThreads / 32; ++w) total += s_wsum[v][w];
-    if (warp == 0) {
+    if (warp == 0 && TPD_INBOUNDS(a.ctl, 1, part, (a.n + kPreThreads - 1) / kPreThreads)) {
         const uint32_t ex = warp_lookback(a.desc, part, total, a.ctl->tag * 16u + 0u, &a.ctl->status, a.spin_limit,
                                           a.never_publish != 0);
         if (lane == 0) {

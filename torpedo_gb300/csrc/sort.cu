@@ -172,7 +172,7 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
         const int cnt = p >= 3 ? 4 : int(p) + 1;
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-            if (j < cnt) d[j] = ld_relaxed_u64(desc + size_t(p - j) * kRadix + digit);
+            if (j < cnt) d[j] = TPD_INBOUNDS(ctl, 10, uint64_t(p - j), part) ? ld_relaxed_u64(desc + size_t(p - j) * kRadix + digit) : make_desc(kFlagPrefix, tag, 0);
         bool stop = false, wait = false;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -198,7 +198,8 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
     return excl;
 }
 
-__global__ void __launch_bounds__(kSortThreads, 3)
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kSortThreads, kMinBlocks)
     onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
                     uint32_t pass, uint32_t shift, uint32_t bits, uint64_t* __restrict__ desc, FrameCtl* ctl,
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(kSortThreads, 3)
 
     // global exclusive digit offsets (histogram of this pass, scanned)
     {
-        const uint32_t h = ctl->sort_hist[pass][tid];
+        const uint32_t h = TPD_INBOUNDS(ctl, 16, pass, 8) ? ctl->sort_hist[pass][tid] : 0u;
         const uint32_t ex = block_exclusive_scan256(h, S.wsum);
         S.gdig[tid] = ex;
     }
@@ -238,15 +239,19 @@ __global__ void __launch_bounds__(kSortThreads, 3)
         bool staged = true;
         if (cnt == kSortTile) {
             if (tid == 0) {
-                mbar_arrive_expect_tx(&S.bar, kSortTile * 12);
-                bulk_copy_g2s(S.keys, keys_in + base, kSortTile * 8, &S.bar);
-                bulk_copy_g2s(S.vals, vals_in + base, kSortTile * 4, &S.bar);
+                const bool ok = TPD_INBOUNDS(ctl, 14, uint64_t(base) + kSortTile, uint64_t(capacity) + 1);
+                mbar_arrive_expect_tx(&S.bar, ok ? kSortTile * 12 : 0u);
+                if (ok) {
+                    bulk_copy_g2s(S.keys, keys_in + base, kSortTile * 8, &S.bar);
+                    bulk_copy_g2s(S.vals, vals_in + base, kSortTile * 4, &S.bar);
+                }
             }
             staged = mbar_wait_bounded(&S.bar, phase, &ctl->status);
             phase ^= 1u;
             staged = __syncthreads_and(staged) != 0;
         } else {
             for (uint32_t j = tid; j < cnt; j += kSortThreads) {
+                if (!TPD_INBOUNDS(ctl, 15, uint64_t(base) + j, capacity)) continue;
                 S.keys[j] = keys_in[base + j];
                 S.vals[j] = vals_in[base + j];
             }
@@ -284,7 +289,7 @@ __global__ void __launch_bounds__(kSortThreads, 3)
             S.whist[w][tid] = count;
             count += c;
         }
-        uint64_t* dp = desc + size_t(part) * kRadix + tid;
+        uint64_t* dp = desc + size_t(TPD_INBOUNDS(ctl, 13, part, nparts) ? part : 0) * kRadix + tid;
         st_relaxed_u64(dp, make_desc(part == 0 ? kFlagPrefix : kFlagAggregate, tag, count));
         const uint32_t lstart = block_exclusive_scan256(count, S.wsum);  // (contains the barrier for whist)
         S.lstart[tid] = lstart;
@@ -303,7 +308,10 @@ __global__ void __launch_bounds__(kSortThreads, 3)
 #pragma unroll
             for (uint32_t i = 0; i < kSortItems; ++i) {
                 const uint32_t d = dr[i] & 511u;
-                if (d < kRadix) S.keys[S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9)] = k[i];
+                if (d < kRadix) {
+                    const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                    if (TPD_INBOUNDS(ctl, 11, pos, cnt)) S.keys[pos] = k[i];
+                }
             }
         }
         {
@@ -317,7 +325,10 @@ __global__ void __launch_bounds__(kSortThreads, 3)
 #pragma unroll
             for (uint32_t i = 0; i < kSortItems; ++i) {
                 const uint32_t d = dr[i] & 511u;
-                if (d < kRadix) S.vals[S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9)] = v[i];
+                if (d < kRadix) {
+                    const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                    if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pos] = v[i];
+                }
             }
         }
 
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(kSortThreads, 3)
                 const uint64_t key = S.keys[j];
                 const uint32_t d = uint32_t(key >> shift) & mask;
                 const uint32_t g = S.gmap[d] + j;
-                if (g < capacity) {
+                if (g < capacity && TPD_INBOUNDS(ctl, 17, g, K + (K == 0))) {
                     keys_out[g] = key;
                     vals_out[g] = S.vals[j];
                 }
@@ -346,7 +357,23 @@ __global__ void __launch_bounds__(kSortThreads, 3)
     }
 }
 
-int g_onesweep_blocks_per_sm = 0;
+
+
+// CTAs per SM the onesweep kernel is compiled for: 2 (128 registers, no
+// spills) or 3 (80 registers). Chosen per engine (tpd_settings.sort_ctas_per_sm).
+int g_onesweep_blocks_per_sm[4] = {0, 0, 0, 0};
+
+template <int kMinBlocks>
+int onesweep_occupancy(size_t smem) {
+    int& b = g_onesweep_blocks_per_sm[kMinBlocks];
+    if (b == 0) {
+        cudaFuncSetAttribute(onesweep_kernel<kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        int r = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kMinBlocks>, kSortThreads, smem);
+        b = r > 0 ? r : 1;
+    }
+    return b;
+}
 
 }  // namespace
 
@@ -360,7 +387,7 @@ void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s) { sort_beg
 
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
                  uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
-                 cudaStream_t s, cudaEvent_t after_hist, bool hist_ready) {
+                 cudaStream_t s, cudaEvent_t after_hist, bool hist_ready, int ctas_per_sm) {
     const uint32_t passes = sort_pass_count(key_bits);
     if (passes == 0 || capacity == 0) return false;
     const int sms = num_sms > 0 ? num_sms : 148;
@@ -371,13 +398,9 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
     }
     if (after_hist) cudaEventRecord(after_hist, s);
     const size_t smem = sizeof(OnesweepSmem);
-    if (g_onesweep_blocks_per_sm == 0) {
-        cudaFuncSetAttribute(onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, onesweep_kernel, kSortThreads, smem);
-        g_onesweep_blocks_per_sm = b > 0 ? b : 1;
-    }
-    const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * g_onesweep_blocks_per_sm)));
+    const int variant = ctas_per_sm == 3 ? 3 : 2;
+    const int occ = variant == 3 ? onesweep_occupancy<3>(smem) : onesweep_occupancy<2>(smem);
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
     uint64_t* kin = keys;
     uint32_t* vin = vals;
     uint64_t* kout = keys_alt;
@@ -385,8 +408,12 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
     for (uint32_t p = 0; p < passes; ++p) {
         const uint32_t shift = p * kRadixBits;
         const uint32_t bits = std::min(kRadixBits, key_bits - shift);
-        onesweep_kernel<<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc, ctl,
-                                                         spin_limit);
+        if (variant == 3)
+            onesweep_kernel<3><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc,
+                                                                ctl, spin_limit);
+        else
+            onesweep_kernel<2><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc,
+                                                                ctl, spin_limit);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

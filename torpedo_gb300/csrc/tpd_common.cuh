@@ -21,6 +21,7 @@ constexpr uint32_t kStatusKeyOverflow = 1u << 0;     // more keys than key capac
 constexpr uint32_t kStatusLookbackTimeout = 1u << 1; // a decoupled look-back spin ran out
 constexpr uint32_t kStatusMbarTimeout = 1u << 2;     // a TMA mbarrier wait ran out
 constexpr uint32_t kStatusBadInput = 1u << 3;        // an input outside the documented range
+constexpr uint32_t kStatusBadIndex = 1u << 4;        // checked builds: an index failed its bounds check
 // Statuses after which the rest of the frame is skipped (its lists are unusable).
 constexpr uint32_t kStatusFatal = kStatusLookbackTimeout | kStatusMbarTimeout;
 
@@ -147,5 +148,23 @@ __device__ __forceinline__ void bounding_rect(float px, float py, float radius, 
 }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// TPD_INBOUNDS(ctl, site, index, bound) guards a computed index: when
+// index >= bound it records (site, index, bound) of the first such event in
+// ctl->debug, raises kStatusBadIndex (the host reports it as an error) and
+// returns false so the caller skips the access. Always compiled in: one
+// compare per guarded access, and inconsistent lists end in an error status
+// instead of an out-of-bounds access.
+template <typename Ctl>
+__device__ __forceinline__ bool tpd_inbounds(Ctl* ctl, uint32_t site, uint64_t index, uint64_t bound) {
+    if (index < bound) return true;
+    if (atomicOr(&ctl->status, kStatusBadIndex) & kStatusBadIndex) return false;
+    ctl->debug[0] = site;
+    ctl->debug[1] = uint32_t(index);
+    ctl->debug[2] = uint32_t(bound);
+    ctl->debug[3] = uint32_t(index >> 32);
+    return false;
+}
+#define TPD_INBOUNDS(ctl, site, index, bound) ::tpd::tpd_inbounds((ctl), (site), (index), (bound))
 
 }  // namespace tpd

@@ -19,7 +19,8 @@ struct FrameCtl {
     uint32_t visible;        // Gaussians with a non-empty tile rect
     uint32_t ticket[16];     // partition tickets, cleared at frame start
     uint32_t sort_hist[8][256];  // per-pass digit counts of the radix sort
-    uint32_t pad[12];
+    uint32_t debug[4];       // checked builds: site, index, bound of the first failed check
+    uint32_t pad[8];
 };
 
 // Entity matrices: rows 0..2 of view*model and rows 0..3 of projview*model.
@@ -79,7 +80,7 @@ uint32_t sort_pass_count(uint32_t key_bits);
 // recorded between the histogram and the first pass.
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
                  uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
-                 cudaStream_t s, cudaEvent_t after_hist = nullptr, bool hist_ready = false);
+                 cudaStream_t s, cudaEvent_t after_hist = nullptr, bool hist_ready = false, int ctas_per_sm = 2);
 // Clears status, sort histograms and tickets, sets total_keys and advances the
 // tag (standalone stage calls).
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s);
@@ -91,7 +92,7 @@ void launch_tile_ranges(const uint64_t* keys, uint32_t n_tiles, uint32_t* ranges
 struct BlendArgs {
     const Splat* splats;      // n_views x n (view-major)
     uint32_t n;               // Gaussians per view
-    const FrameCtl* ctl;      // K = min(ctl->total_keys, capacity); frames with a fatal status are skipped
+    FrameCtl* ctl;            // K = min(ctl->total_keys, capacity); frames with a fatal status are skipped
     uint32_t capacity;
     const uint32_t* vals;
     const uint32_t* ranges;   // 2 x n_tiles (global tile ids)
@@ -112,7 +113,7 @@ void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStre
 struct BlendBackwardArgs {
     const Splat* splats;      // n_views x n (view-major)
     uint32_t n;               // Gaussians per view
-    const FrameCtl* ctl;
+    FrameCtl* ctl;
     uint32_t capacity;
     const uint32_t* vals;
     const uint32_t* ranges;
