@@ -253,7 +253,8 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
         mbar_arrive_expect_tx(&bar, bytes);
         bulk_copy_g2s(srec, a.recs + size_t(base) * kRecordFloats, bytes, &bar);
     }
-    const bool staged = mbar_wait_bounded(&bar, 0, &a.ctl->status);
+    bool staged = mbar_wait_bounded(&bar, 0, &a.ctl->status);
+    if (!staged) mbar_wait_bounded(&bar, 0, &a.ctl->status, 1u << 26);  // never leave with the copy in flight
 
     const uint32_t i = base + tid;
     const uint32_t e = (tid < cnt && a.ent_idx) ? a.ent_idx[i] : 0u;

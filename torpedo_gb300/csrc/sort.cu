@@ -8,17 +8,18 @@
 //
 // GB300 form (onesweep): 8-bit digits, so a 45-bit (tile | depth) key takes 6
 // passes instead of 23.
-//  1. sort_histogram_kernel reads every key once, staging 16 KB chunks into
-//     shared memory with TMA bulk copies (double buffered), and builds the
-//     digit histograms of all passes at once (warp match-any aggregation into
-//     shared memory, one global atomic per bin per CTA).
+//  1. The digit histograms of all passes come from key duplication (keygen.cu)
+//     in the pipeline; sort_histogram_kernel builds them for standalone sorts
+//     (one read of the keys, warp match-any aggregation into shared memory,
+//     one global atomic per bin per CTA).
 //  2. onesweep_kernel, once per pass: a persistent CTA takes 4096-key
-//     partitions by atomic ticket, stages keys and values with TMA, ranks keys
-//     per warp (match-any, stable within the warp-striped order), combines
-//     warps per digit, resolves each digit's global prefix by a decoupled
-//     look-back over predecessor partitions (one thread per digit, bounded
-//     spin), reorders the partition in shared memory and writes digit runs
-//     out coalesced.
+//     partitions by atomic ticket, loads them with coalesced warp-striped
+//     loads, ranks keys per warp (match-any, stable within the warp-striped
+//     order), combines warps per digit, publishes its digit counts, reorders
+//     the partition in shared memory while predecessors publish, resolves
+//     each digit's global prefix by a decoupled look-back (one thread per
+//     digit, four predecessors per round trip, bounded spin) and writes digit
+//     runs out coalesced.
 // The result is the stable sort of the pairs by the low key_bits bits, the
 // same permutation as the reference's sort.
 #include <algorithm>
@@ -49,7 +50,6 @@ struct OnesweepSmem {
     uint32_t lstart[kRadix];  // block-local digit start
     uint32_t gmap[kRadix];    // global position of local index 0 of each digit
     uint32_t wsum[kSortWarps];
-    uint64_t bar;
     uint32_t part;
 };
 
@@ -57,10 +57,6 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
-}
-
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Block-wide exclusive scan of one value per thread (256 threads); returns the exclusive prefix.
@@ -98,18 +94,10 @@ __global__ void __launch_bounds__(kHistThreads)
     sort_histogram_kernel(const uint64_t* __restrict__ keys, uint32_t capacity, uint32_t passes, uint32_t key_bits,
                           FrameCtl* ctl) {
     __shared__ uint32_t sh[8][kRadix];
-    __shared__ __align__(128) uint64_t stage[2][kHistChunk];
-    __shared__ __align__(8) uint64_t bar[2];
     const uint32_t tid = threadIdx.x;
     for (uint32_t i = tid; i < 8 * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        fence_mbar_init();
-    }
     __syncthreads();
     const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(ctl->total_keys, capacity);
-    const uint32_t nfull = K / kHistChunk;  // full chunks go through TMA
     uint32_t shift[8], mask[8];
 #pragma unroll
     for (uint32_t p = 0; p < 8; ++p) {
@@ -117,39 +105,15 @@ __global__ void __launch_bounds__(kHistThreads)
         const uint32_t b = (p * kRadixBits < key_bits) ? min(kRadixBits, key_bits - p * kRadixBits) : 0u;
         mask[p] = (1u << b) - 1u;
     }
-    auto issue = [&](uint32_t c, uint32_t st) {
-        mbar_arrive_expect_tx(&bar[st], kHistChunk * 8);
-        bulk_copy_g2s(stage[st], keys + size_t(c) * kHistChunk, kHistChunk * 8, &bar[st]);
-    };
-    uint32_t c = blockIdx.x;
-    if (tid == 0) {
-        if (c < nfull) issue(c, 0);
-        if (c + gridDim.x < nfull) issue(c + gridDim.x, 1);
-    }
-    uint32_t phase[2] = {0, 0};
-    uint32_t it = 0;
-    for (; c < nfull; c += gridDim.x, ++it) {
-        const uint32_t st = it & 1u;
-        const bool ok = mbar_wait_bounded(&bar[st], phase[st], &ctl->status);
-        phase[st] ^= 1u;
-        if (ok) {
+    // grid-stride over chunks of kHistChunk keys; the trip count is uniform per CTA
+    const uint32_t nchunks = (K + kHistChunk - 1) / kHistChunk;
+    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint32_t base = c * kHistChunk;
 #pragma unroll 2
-            for (uint32_t j = tid; j < kHistChunk; j += kHistThreads) {
-                const uint64_t k = stage[st][j];
-                for (uint32_t p = 0; p < passes; ++p) hist_add(sh[p], uint32_t(k >> shift[p]) & mask[p]);
-            }
-        }
-        fence_proxy_async_smem();
-        __syncthreads();  // stage[st] free again
-        if (tid == 0 && c + 2 * gridDim.x < nfull) issue(c + 2 * gridDim.x, st);
-    }
-    // tail keys (fewer than one chunk) with plain loads, by CTA 0
-    if (blockIdx.x == 0) {
-        const uint32_t tail0 = nfull * kHistChunk;
-        const uint32_t tail_end = tail0 + (K - tail0 + kHistThreads - 1) / kHistThreads * kHistThreads;
-        for (uint32_t j = tail0 + tid; j < tail_end; j += kHistThreads) {  // uniform trip count
-            const bool v = j < K;
-            const uint64_t k = v ? keys[j] : 0ull;
+        for (uint32_t j = tid; j < kHistChunk; j += kHistThreads) {
+            const uint32_t idx = base + j;
+            const bool v = idx < K;
+            const uint64_t k = v ? keys[idx] : 0ull;
             for (uint32_t p = 0; p < passes; ++p)
                 hist_add(sh[p], v ? (uint32_t(k >> shift[p]) & mask[p]) : kInvalidDigit);
         }
@@ -218,14 +182,8 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         const uint32_t ex = block_exclusive_scan256(h, S.wsum);
         S.gdig[tid] = ex;
     }
-    if (tid == 0) {
-        mbar_init(&S.bar, 1);
-        fence_mbar_init();
-    }
-    uint32_t phase = 0;
 
     while (true) {
-        fence_proxy_async_smem();
         if (tid == 0) S.part = atomicAdd(&ctl->ticket[kTicketSortBase + pass], 1u);
 #pragma unroll
         for (uint32_t w = 0; w < kSortWarps; ++w) S.whist[w][tid] = 0;
@@ -235,39 +193,22 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         const uint32_t base = part * kSortTile;
         const uint32_t cnt = min(kSortTile, K - base);
 
-        // stage the partition
-        bool staged = true;
-        if (cnt == kSortTile) {
-            if (tid == 0) {
-                const bool ok = TPD_INBOUNDS(ctl, 14, uint64_t(base) + kSortTile, uint64_t(capacity) + 1);
-                mbar_arrive_expect_tx(&S.bar, ok ? kSortTile * 12 : 0u);
-                if (ok) {
-                    bulk_copy_g2s(S.keys, keys_in + base, kSortTile * 8, &S.bar);
-                    bulk_copy_g2s(S.vals, vals_in + base, kSortTile * 4, &S.bar);
-                }
-            }
-            staged = mbar_wait_bounded(&S.bar, phase, &ctl->status);
-            phase ^= 1u;
-            staged = __syncthreads_and(staged) != 0;
-        } else {
-            for (uint32_t j = tid; j < cnt; j += kSortThreads) {
-                if (!TPD_INBOUNDS(ctl, 15, uint64_t(base) + j, capacity)) continue;
-                S.keys[j] = keys_in[base + j];
-                S.vals[j] = vals_in[base + j];
-            }
-            __syncthreads();
+        // Warp-striped items, loaded coalesced straight from global memory: warp
+        // w owns [w*512, w*512+512), item i covers 32 consecutive keys. dr[i]
+        // packs the digit (bits 0..8, kInvalidDigit past K) and the key's rank
+        // among equal digits earlier in the warp (bits 9..31).
+        uint64_t k[kSortItems];
+#pragma unroll
+        for (uint32_t i = 0; i < kSortItems; ++i) {
+            const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
+            k[i] = idx < cnt ? keys_in[base + idx] : ~0ull;
         }
-
-        // Warp-striped items: warp w owns [w*512, w*512+512), item i covers 32
-        // consecutive keys. dr[i] packs the digit (bits 0..8, kInvalidDigit for
-        // keys past K) and the key's rank among equal digits earlier in the
-        // warp (bits 9..31); keys themselves are re-read from shared memory.
         uint32_t dr[kSortItems];
         const uint32_t lt = lanemask_lt();
 #pragma unroll
         for (uint32_t i = 0; i < kSortItems; ++i) {
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-            const uint32_t d = (idx < cnt && staged) ? (uint32_t(S.keys[idx] >> shift) & mask) : kInvalidDigit;
+            const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
             const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
             const uint32_t leader = __ffs(peers) - 1;
             uint32_t prev = 0;
@@ -291,44 +232,28 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         }
         uint64_t* dp = desc + size_t(TPD_INBOUNDS(ctl, 13, part, nparts) ? part : 0) * kRadix + tid;
         st_relaxed_u64(dp, make_desc(part == 0 ? kFlagPrefix : kFlagAggregate, tag, count));
-        const uint32_t lstart = block_exclusive_scan256(count, S.wsum);  // (contains the barrier for whist)
+        const uint32_t lstart = block_exclusive_scan256(count, S.wsum);  // (its barriers cover whist)
         S.lstart[tid] = lstart;
         __syncthreads();
 
         // reorder the partition in shared memory (stable: warp, then item, then
-        // lane) while predecessors publish; keys first, then values
-        {
-            uint64_t k[kSortItems];
+        // lane) while predecessors publish; values are loaded now, coalesced
 #pragma unroll
-            for (uint32_t i = 0; i < kSortItems; ++i) {
-                const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-                k[i] = S.keys[min(idx, kSortTile - 1)];
-            }
-            __syncthreads();
-#pragma unroll
-            for (uint32_t i = 0; i < kSortItems; ++i) {
-                const uint32_t d = dr[i] & 511u;
-                if (d < kRadix) {
-                    const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-                    if (TPD_INBOUNDS(ctl, 11, pos, cnt)) S.keys[pos] = k[i];
-                }
+        for (uint32_t i = 0; i < kSortItems; ++i) {
+            const uint32_t d = dr[i] & 511u;
+            if (d < kRadix) {
+                const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                if (TPD_INBOUNDS(ctl, 11, pos, cnt)) S.keys[pos] = k[i];
             }
         }
-        {
-            uint32_t v[kSortItems];
 #pragma unroll
-            for (uint32_t i = 0; i < kSortItems; ++i) {
-                const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-                v[i] = S.vals[min(idx, kSortTile - 1)];
-            }
-            __syncthreads();
-#pragma unroll
-            for (uint32_t i = 0; i < kSortItems; ++i) {
-                const uint32_t d = dr[i] & 511u;
-                if (d < kRadix) {
-                    const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-                    if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pos] = v[i];
-                }
+        for (uint32_t i = 0; i < kSortItems; ++i) {
+            const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
+            const uint32_t d = dr[i] & 511u;
+            if (d < kRadix) {
+                const uint32_t v = vals_in[base + idx];
+                const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pos] = v;
             }
         }
 
@@ -343,21 +268,18 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         __syncthreads();
 
         // coalesced write-out of digit runs
-        if (staged) {
-            for (uint32_t j = tid; j < cnt; j += kSortThreads) {
-                const uint64_t key = S.keys[j];
-                const uint32_t d = uint32_t(key >> shift) & mask;
-                const uint32_t g = S.gmap[d] + j;
-                if (g < capacity && TPD_INBOUNDS(ctl, 17, g, K + (K == 0))) {
-                    keys_out[g] = key;
-                    vals_out[g] = S.vals[j];
-                }
+        for (uint32_t j = tid; j < cnt; j += kSortThreads) {
+            const uint64_t key = S.keys[j];
+            const uint32_t d = uint32_t(key >> shift) & mask;
+            const uint32_t g = S.gmap[d] + j;
+            if (g < capacity && TPD_INBOUNDS(ctl, 17, g, K + (K == 0))) {
+                keys_out[g] = key;
+                vals_out[g] = S.vals[j];
             }
         }
+        __syncthreads();  // S.keys / S.vals / S.gmap are rewritten by the next partition
     }
 }
-
-
 
 // CTAs per SM the onesweep kernel is compiled for: 2 (128 registers, no
 // spills) or 3 (80 registers). Chosen per engine (tpd_settings.sort_ctas_per_sm).
