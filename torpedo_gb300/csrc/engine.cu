@@ -87,7 +87,7 @@ struct tpd_engine {
     uint64_t capacity = 0;
     uint64_t* d_keys[2] = {nullptr, nullptr};
     uint32_t* d_vals[2] = {nullptr, nullptr};
-    uint32_t* d_desc_sort = nullptr;
+    uint64_t* d_desc_sort = nullptr;
     uint32_t* d_ranges = nullptr;
     uint64_t pixel_cap = 0, tile_cap = 0;
     float* d_image = nullptr;
@@ -178,7 +178,7 @@ int ensure_splat_buffers(tpd_engine* e) {
 
 int ensure_key_capacity(tpd_engine* e, uint64_t want) {
     if (want <= e->capacity) return TPD_OK;
-    if (want >= (1ull << 30)) return fail(e, TPD_ERR_CAPACITY, "key count must stay below 2^30");
+    if (want > 0x7FFFFFFFull) return fail(e, TPD_ERR_CAPACITY, "key count exceeds 2^31-1");
     invalidate_graph(e);
     for (int b = 0; b < 2; ++b) {
         TPD_CUDA(e, dalloc(e->d_keys[b], want));
@@ -186,7 +186,7 @@ int ensure_key_capacity(tpd_engine* e, uint64_t want) {
     }
     const size_t entries = sort_desc_entries(uint32_t(want));
     TPD_CUDA(e, dalloc(e->d_desc_sort, entries));
-    TPD_CUDA(e, cudaMemset(e->d_desc_sort, 0, entries * 4));
+    TPD_CUDA(e, cudaMemset(e->d_desc_sort, 0, entries * 8));
     e->capacity = want;
     return TPD_OK;
 }
@@ -817,7 +817,7 @@ void* tpd_get_stream(const tpd_engine* e) { return e ? static_cast<void*>(e->str
 // ---- stage entry points
 
 size_t tpd_sort_workspace_size(uint32_t n) {
-    return 256 * ((sizeof(FrameCtl) + 255) / 256) + sort_desc_entries(n) * 4;
+    return 256 * ((sizeof(FrameCtl) + 255) / 256) + sort_desc_entries(n) * 8;
 }
 
 int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t n,
@@ -826,15 +826,15 @@ int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t*
     *result_in_alt = 0;
     if (n == 0) return TPD_OK;
     if (!keys || !vals || !keys_alt || !vals_alt || !workspace) return TPD_ERR_ARG;
-    if (key_bits == 0 || key_bits > 64 || n >= (1u << 30)) return TPD_ERR_ARG;
+    if (key_bits == 0 || key_bits > 64 || n > 0x7FFFFFFFu) return TPD_ERR_ARG;
     if (workspace_bytes < tpd_sort_workspace_size(n)) return TPD_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     FrameCtl* ctl = static_cast<FrameCtl*>(workspace);
-    uint32_t* desc = reinterpret_cast<uint32_t*>(static_cast<char*>(workspace) + 256 * ((sizeof(FrameCtl) + 255) / 256));
+    uint64_t* desc = reinterpret_cast<uint64_t*>(static_cast<char*>(workspace) + 256 * ((sizeof(FrameCtl) + 255) / 256));
     int sms = 148, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaMemsetAsync(desc, 0, sort_desc_entries(n) * 4, s) != cudaSuccess) return TPD_ERR_DEVICE;
+    if (cudaMemsetAsync(desc, 0, sort_desc_entries(n) * 8, s) != cudaSuccess) return TPD_ERR_DEVICE;
     launch_sort_begin(ctl, n, s);
     const bool alt = launch_sort(keys, vals, keys_alt, vals_alt, n, key_bits, desc, ctl, kDefaultSpin, sms, s);
     *result_in_alt = alt ? 1 : 0;

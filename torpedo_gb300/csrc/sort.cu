@@ -124,61 +124,33 @@ __global__ void __launch_bounds__(kHistThreads)
             if (sh[p][d]) atomicAdd(&ctl->sort_hist[p][d], sh[p][d]);
 }
 
-// Sort look-back descriptors: 32 bits, [31:30] flag (0 unpublished,
-// 1 aggregate, 2 inclusive prefix), [29:0] count. Stored digit-major,
-// desc[digit * dstride + partition], so one digit's predecessors are
-// contiguous: a thread reads 64 of them (two 128-byte lines) per round trip.
-// Two regions alternate between passes; each pass clears the other region's
-// entries of the partitions it processes (the next pass has the same
-// partitions), and region 0 is cleared once at the start of a sort.
-constexpr uint32_t kDescWindow = 64;
-constexpr uint32_t kDescAggregate = 1u << 30;
-constexpr uint32_t kDescPrefix = 2u << 30;
-constexpr uint32_t kDescValue = (1u << 30) - 1u;
-
-__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ uint4 ld_relaxed_v4(const uint32_t* p) {
-    uint4 v;
-    asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p)
-                 : "memory");
-    return v;
-}
-
-// Exclusive prefix of partition `part` for one digit; row = desc + digit * dstride.
-__device__ __forceinline__ uint32_t digit_lookback(const uint32_t* __restrict__ row, uint32_t part, FrameCtl* ctl,
-                                                   uint32_t spin_limit) {
+// Resolves the exclusive prefix of one digit for partition `part` by walking
+// predecessors; up to four descriptors are loaded per round trip.
+__device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ desc, uint32_t part, uint32_t digit,
+                                                   uint32_t tag, FrameCtl* ctl, uint32_t spin_limit) {
     uint32_t excl = 0;
-    int32_t hi = int32_t(part);  // entries [0, hi) are still to be accounted
+    int64_t p = int64_t(part) - 1;
     uint32_t spins = 0;
-    while (hi > 0) {
-        const int32_t blk = (hi - 1) & ~int32_t(kDescWindow - 1);
-        uint32_t w[kDescWindow];
+    while (p >= 0) {
+        uint64_t d[4];
+        const int cnt = p >= 3 ? 4 : int(p) + 1;
 #pragma unroll
-        for (uint32_t q = 0; q < kDescWindow / 4; ++q) {
-            const uint4 v = ld_relaxed_v4(row + blk + 4 * q);
-            w[4 * q + 0] = v.x;
-            w[4 * q + 1] = v.y;
-            w[4 * q + 2] = v.z;
-            w[4 * q + 3] = v.w;
-        }
-        bool done = false, wait = false;
+        for (int j = 0; j < 4; ++j)
+            if (j < cnt) d[j] = TPD_INBOUNDS(ctl, 10, uint64_t(p - j), part) ? ld_relaxed_u64(desc + size_t(p - j) * kRadix + digit) : make_desc(kFlagPrefix, tag, 0);
+        bool stop = false, wait = false;
 #pragma unroll
-        for (int32_t j = int32_t(kDescWindow) - 1; j >= 0; --j) {
-            if (done || wait || blk + j >= hi) continue;
-            const uint32_t d = w[j];
-            if (d == 0u) {
-                wait = true;  // not yet published: re-read from here
+        for (int j = 0; j < 4; ++j) {
+            if (j >= cnt || stop || wait) continue;
+            const uint32_t f = desc_flag(d[j], tag);
+            if (f == 0u) {
+                wait = true;  // not yet published: retry from here
             } else {
-                excl += d & kDescValue;
-                hi = blk + j;
-                if (d & kDescPrefix) done = true;
+                excl += uint32_t(d[j]);
+                --p;
+                if (f == uint32_t(kFlagPrefix)) stop = true;
             }
         }
-        if (done) break;
+        if (stop) break;
         if (wait) {
             if (++spins > spin_limit) {
                 atomicOr(&ctl->status, kStatusLookbackTimeout);
@@ -194,13 +166,14 @@ template <int kMinBlocks>
 __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
     onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
-                    uint32_t pass, uint32_t shift, uint32_t bits, uint32_t* __restrict__ desc,
-                    uint32_t* __restrict__ desc_next, uint32_t dstride, FrameCtl* ctl, uint32_t spin_limit) {
+                    uint32_t pass, uint32_t shift, uint32_t bits, uint64_t* __restrict__ desc, FrameCtl* ctl,
+                    uint32_t spin_limit) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     OnesweepSmem& S = *reinterpret_cast<OnesweepSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(ctl->total_keys, capacity);
     const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
+    const uint32_t tag = ctl->tag * 16u + 1u + pass;
     const uint32_t mask = (1u << bits) - 1u;
 
     // global exclusive digit offsets (histogram of this pass, scanned)
@@ -257,10 +230,8 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
             S.whist[w][tid] = count;
             count += c;
         }
-        const uint32_t slot = TPD_INBOUNDS(ctl, 13, part, dstride) ? part : 0u;
-        uint32_t* row = desc + size_t(tid) * dstride;
-        st_relaxed_u32(row + slot, (part == 0 ? kDescPrefix : kDescAggregate) | count);
-        desc_next[size_t(tid) * dstride + slot] = 0u;  // the next pass starts from cleared descriptors
+        uint64_t* dp = desc + size_t(TPD_INBOUNDS(ctl, 13, part, nparts) ? part : 0) * kRadix + tid;
+        st_relaxed_u64(dp, make_desc(part == 0 ? kFlagPrefix : kFlagAggregate, tag, count));
         const uint32_t lstart = block_exclusive_scan256(count, S.wsum);  // (its barriers cover whist)
         S.lstart[tid] = lstart;
         __syncthreads();
@@ -288,8 +259,8 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
 
         // decoupled look-back for this thread's digit
         if (part > 0) {
-            const uint32_t excl = digit_lookback(row, part, ctl, spin_limit);
-            st_relaxed_u32(row + slot, kDescPrefix | ((excl + count) & kDescValue));
+            const uint32_t excl = digit_lookback(desc, part, tid, tag, ctl, spin_limit);
+            st_relaxed_u64(dp, make_desc(kFlagPrefix, tag, excl + count));
             S.gmap[tid] = S.gdig[tid] + excl - lstart;
         } else {
             S.gmap[tid] = S.gdig[tid] - lstart;
@@ -330,19 +301,14 @@ int onesweep_occupancy(size_t smem) {
 
 uint32_t sort_pass_count(uint32_t key_bits) { return (key_bits + kRadixBits - 1) / kRadixBits; }
 
-uint32_t sort_desc_stride(uint32_t capacity) {
-    const uint32_t parts = (capacity + kSortTile - 1) / kSortTile;
-    return (parts + kDescWindow) & ~(kDescWindow - 1);  // room for the partitions, a multiple of the window
+size_t sort_desc_entries(uint32_t capacity) {
+    return (size_t(capacity) + kSortTile - 1) / kSortTile * kRadix + kRadix;
 }
-
-size_t sort_desc_entries(uint32_t capacity) { return size_t(2) * kRadix * sort_desc_stride(capacity); }
-
-size_t sort_desc_region0_bytes(uint32_t capacity) { return size_t(kRadix) * sort_desc_stride(capacity) * 4; }
 
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s) { sort_begin_kernel<<<1, 256, 0, s>>>(ctl, total); }
 
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
-                 uint32_t key_bits, uint32_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
                  cudaStream_t s, cudaEvent_t after_hist, bool hist_ready, int ctas_per_sm) {
     const uint32_t passes = sort_pass_count(key_bits);
     if (passes == 0 || capacity == 0) return false;
@@ -357,9 +323,6 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
     const int variant = ctas_per_sm == 3 ? 3 : 2;
     const int occ = variant == 3 ? onesweep_occupancy<3>(smem) : onesweep_occupancy<2>(smem);
     const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
-    const uint32_t dstride = sort_desc_stride(capacity);
-    uint32_t* region[2] = {desc, desc + size_t(kRadix) * dstride};
-    cudaMemsetAsync(region[0], 0, size_t(kRadix) * dstride * 4, s);
     uint64_t* kin = keys;
     uint32_t* vin = vals;
     uint64_t* kout = keys_alt;
@@ -367,14 +330,12 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
     for (uint32_t p = 0; p < passes; ++p) {
         const uint32_t shift = p * kRadixBits;
         const uint32_t bits = std::min(kRadixBits, key_bits - shift);
-        uint32_t* cur = region[p & 1u];
-        uint32_t* nxt = region[(p + 1) & 1u];
         if (variant == 3)
-            onesweep_kernel<3><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, cur,
-                                                                nxt, dstride, ctl, spin_limit);
+            onesweep_kernel<3><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc,
+                                                                ctl, spin_limit);
         else
-            onesweep_kernel<2><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, cur,
-                                                                nxt, dstride, ctl, spin_limit);
+            onesweep_kernel<2><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc,
+                                                                ctl, spin_limit);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

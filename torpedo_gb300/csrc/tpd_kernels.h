@@ -73,13 +73,13 @@ void launch_keygen(const Splat* splats, const uint32_t* offsets, uint32_t n, con
 // K = min(ctl->total_keys, capacity). Result in (keys, vals) if the pass count
 // is even, else in (keys_alt, vals_alt); returns true when it is in *_alt.
 // desc: sort_desc_entries(capacity) descriptors.
-size_t sort_desc_entries(uint32_t capacity);  // u32 descriptors (two regions)
+size_t sort_desc_entries(uint32_t capacity);
 uint32_t sort_pass_count(uint32_t key_bits);
 // hist_ready: ctl->sort_hist already holds the digit histograms (keygen built
 // them), so the histogram kernel is skipped. after_hist (nullable): event
 // recorded between the histogram and the first pass.
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
-                 uint32_t key_bits, uint32_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
                  cudaStream_t s, cudaEvent_t after_hist = nullptr, bool hist_ready = false, int ctas_per_sm = 2);
 // Clears status, sort histograms and tickets, sets total_keys and advances the
 // tag (standalone stage calls).
