@@ -72,10 +72,10 @@ typedef struct tpd_settings {
 
 /* Stages of a frame, for tpd_stage_times. */
 enum {
-    TPD_STAGE_PREPROCESS = 0, /* camera upload, entity matrices, preprocess + tile-count scan */
-    TPD_STAGE_KEYGEN = 1,     /* key duplication */
-    TPD_STAGE_SORT_HIST = 2,  /* radix sort: digit histograms of all passes */
-    TPD_STAGE_SORT_PASSES = 3,/* radix sort: all onesweep passes */
+    TPD_STAGE_PREPROCESS = 0, /* camera upload, entity matrices, preprocess (splats + depth keys) */
+    TPD_STAGE_DEPTH_SORT = 1, /* radix sort of the (view | depth) keys, tile-count scan in depth order */
+    TPD_STAGE_KEYGEN = 2,     /* key duplication in depth order */
+    TPD_STAGE_KEY_SORT = 3,   /* radix sort of the (tile | depth) keys on their tile-id bits */
     TPD_STAGE_RANGES = 4,     /* tile ranges (clear + kernel) */
     TPD_STAGE_BLEND = 5,      /* alpha blend */
     TPD_STAGE_COUNT = 6

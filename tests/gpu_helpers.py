@@ -53,7 +53,14 @@ def oracle_frame(records, cam, sh_degree=3, band3_compat=True, ent_idx=None, tra
     skeys, svals = O.stable_sort(keys, vals)
     n_tiles = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
     rng = O.tile_ranges(skeys, n_tiles)
-    out = dict(s32=s32, offsets=offs, K=k, keys_unsorted=keys, vals_unsorted=vals, keys=skeys, vals=svals, ranges=rng)
+    # key offsets in depth order (the engine scans tile counts after sorting the
+    # Gaussians by (depth bits, index); culled ones, depth key 0xFFFFFFFF, go last)
+    dkey = np.where(s32[:, 3] > 0, s32[:, 6], np.uint32(0xFFFFFFFF)).astype(np.uint32)
+    order = np.argsort(dkey, kind="stable")
+    cnt = s32[order, 3].astype(np.uint64)
+    doffs = (np.cumsum(cnt) - cnt).astype(np.uint32)
+    out = dict(s32=s32, offsets=offs, depth_offsets=doffs, K=k, keys_unsorted=keys, vals_unsorted=vals, keys=skeys,
+               vals=svals, ranges=rng)
     if f64:
         s64, rect, frag = O.preprocess_f64(records, oc, sh_degree, band3_compat, ent_idx, transforms)
         img64, T64, nc64, pfrag = O.blend_f64(s64, svals, rng, cam.width, cam.height)

@@ -3,7 +3,7 @@
   preprocess   bit-exact vs the FP32 transcription; <= 1e-5 scaled relative
                error vs FP64 (tests/tolerances.py); tile counts exact except
                the FP64 oracle's edge set, which is counted and reported
-  scan         offsets and K exact
+  scan         K exact; key offsets exact (scanned in depth order)
   keygen+sort  keys and values bit-exact vs keygen + std::stable_sort
   ranges       bit-exact
   blend        <= 1e-3 max-abs per channel vs FP64, outside flagged pixels
@@ -79,7 +79,7 @@ def test_splats_vs_fp64(frame):
 def test_scan_offsets_and_total(frame):
     recs, cam, stats, g, o = frame
     assert stats["keys"] == o["K"]
-    np.testing.assert_array_equal(g["offsets"], o["offsets"])
+    np.testing.assert_array_equal(g["offsets"], o["depth_offsets"])
     assert stats["visible"] == int((o["s32"][:, 3] > 0).sum())
 
 

@@ -12,7 +12,7 @@ _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libtpdsplat.so"
 
 TPD_OK, TPD_ERR_ARG, TPD_ERR_OOM, TPD_ERR_TIMEOUT, TPD_ERR_DEVICE, TPD_ERR_STATE, TPD_ERR_CAPACITY, TPD_ERR_IO = range(8)
 TPD_IMAGE_RGB32F, TPD_IMAGE_RGBA8 = 0, 1
-STAGES = ("preprocess", "keygen", "sort_hist", "sort_passes", "ranges", "blend")
+STAGES = ("preprocess", "depth_sort", "keygen", "key_sort", "ranges", "blend")
 (TPD_BUF_RECORDS, TPD_BUF_SPLATS, TPD_BUF_OFFSETS, TPD_BUF_KEYS, TPD_BUF_VALUES, TPD_BUF_RANGES, TPD_BUF_IMAGE,
  TPD_BUF_FINAL_T, TPD_BUF_N_CONTRIB, TPD_BUF_G2D) = range(10)
 

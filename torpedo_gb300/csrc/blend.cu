@@ -25,7 +25,6 @@ namespace tpd {
 namespace {
 
 constexpr uint32_t kBlendThreads = kTilePixels;  // 256
-constexpr float kAlphaMin = 1.0f / 255.0f;
 constexpr float kAlphaMax = 0.99f;
 constexpr float kTMin = 0.0001f;
 

@@ -32,7 +32,6 @@ using namespace tpd;
 namespace {
 
 constexpr uint32_t kDefaultSpin = 1u << 20;
-constexpr uint32_t kPreThreads = 128;
 constexpr uint32_t kScanTileStandalone = 1024;
 
 struct StatsHead {
@@ -77,9 +76,14 @@ struct tpd_engine {
     uint64_t* d_image_offset = nullptr;
 
     // frame buffers
-    uint64_t splat_cap = 0;  // entries of splats / offsets (views x n)
+    uint64_t splat_cap = 0;  // entries of splats / offsets / depth keys (views x n)
     Splat* d_splats = nullptr;
-    uint32_t* d_offsets = nullptr;
+    uint32_t* d_offsets = nullptr;  // key offsets of the items in depth order
+    uint64_t* d_dkeys[2] = {nullptr, nullptr};
+    uint32_t* d_ditems[2] = {nullptr, nullptr};
+    uint64_t* d_desc_depth = nullptr;
+    uint32_t depth_key_bits = 32;
+    bool depth_in_alt = false;
     uint64_t* d_desc_pre = nullptr;
     uint64_t desc_pre_cap = 0;
     float* d_ent_mats = nullptr;
@@ -158,9 +162,16 @@ int ensure_splat_buffers(tpd_engine* e) {
         invalidate_graph(e);
         TPD_CUDA(e, dalloc(e->d_splats, need));
         TPD_CUDA(e, dalloc(e->d_offsets, need));
+        for (int b = 0; b < 2; ++b) {
+            TPD_CUDA(e, dalloc(e->d_dkeys[b], need));
+            TPD_CUDA(e, dalloc(e->d_ditems[b], need));
+        }
+        const size_t de = sort_desc_entries(uint32_t(need));
+        TPD_CUDA(e, dalloc(e->d_desc_depth, de));
+        TPD_CUDA(e, cudaMemset(e->d_desc_depth, 0, de * 8));
         e->splat_cap = need;
     }
-    const uint64_t parts = (uint64_t(e->n) + kPreThreads - 1) / kPreThreads + 1;
+    const uint64_t parts = need / kScanTileStandalone + 2;
     if (parts > e->desc_pre_cap) {
         invalidate_graph(e);
         TPD_CUDA(e, dalloc(e->d_desc_pre, parts));
@@ -243,7 +254,7 @@ void enqueue_frame(tpd_engine* e) {
     }();
     cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(s, &cap_status);
-    static const char* kStageNames[] = {"begin", "preprocess", "keygen", "sort", "sort", "ranges", "blend"};
+    static const char* kStageNames[] = {"begin", "preprocess", "depth sort", "keygen", "key sort", "ranges", "blend"};
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], s);
         if (debug_sync && cap_status == cudaStreamCaptureStatusNone) {
@@ -269,20 +280,43 @@ void enqueue_frame(tpd_engine* e) {
     pa.sh_degree = e->settings.sh_degree;
     pa.band3_compat = e->settings.band3_compat;
     pa.splats = e->d_splats;
-    pa.offsets = e->d_offsets;
-    pa.desc = e->d_desc_pre;
+    pa.depth_keys = e->d_dkeys[0];
+    pa.depth_items = e->d_ditems[0];
+    pa.depth_key_bits = e->depth_key_bits;
     pa.ctl = e->d_ctl;
-    pa.spin_limit = e->settings.spin_limit ? e->settings.spin_limit : kDefaultSpin;
-    pa.never_publish = e->settings.test_never_publish;
     launch_preprocess(pa, s);
     mark(1);
-    const uint32_t cap = uint32_t(e->capacity);
-    launch_keygen(e->d_splats, e->d_offsets, e->n, e->d_views, e->n_views, e->d_keys[0], e->d_vals[0], cap,
-                  e->key_bits, e->d_ctl, e->num_sms, s);
+    const uint32_t spin = e->settings.spin_limit ? e->settings.spin_limit : kDefaultSpin;
+    const uint32_t items = e->n * e->n_views;
+    SortPlan dp;
+    dp.first_bit = 0;
+    dp.key_bits = e->depth_key_bits;
+    dp.hist = e->d_ctl->depth_hist;
+    dp.hist_ready = true;
+    dp.ticket_base = kTicketDepthSortBase;
+    dp.tag_base = kTagDepthSort;
+    dp.ctas_per_sm = int(e->settings.sort_ctas_per_sm);
+    dp.fixed_count = items;
+    e->depth_in_alt = launch_sort(e->d_dkeys[0], e->d_ditems[0], e->d_dkeys[1], e->d_ditems[1], items, dp,
+                                  e->d_desc_depth, e->d_ctl, spin, e->num_sms, s);
+    const uint32_t* order = e->d_ditems[e->depth_in_alt ? 1 : 0];
+    launch_depth_scan(e->d_splats, order, items, e->d_offsets, e->d_desc_pre, e->d_ctl, spin,
+                      e->settings.test_never_publish, s);
     mark(2);
-    e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, e->key_bits,
-                                   e->d_desc_sort, e->d_ctl, pa.spin_limit, e->num_sms, s, ev ? ev[3] : nullptr,
-                                   /*hist_ready=*/true, int(e->settings.sort_ctas_per_sm));
+    const uint32_t cap = uint32_t(e->capacity);
+    launch_keygen(e->d_splats, order, e->d_offsets, items, e->n, e->d_views, e->d_keys[0], e->d_vals[0], cap,
+                  e->key_bits, e->d_ctl, e->num_sms, s);
+    mark(3);
+    SortPlan kp;
+    kp.first_bit = 32;  // the low 32 bits (depth) are already in order
+    kp.key_bits = e->key_bits;
+    kp.hist = e->d_ctl->sort_hist;
+    kp.hist_ready = true;
+    kp.ticket_base = kTicketKeySortBase;
+    kp.tag_base = kTagKeySort;
+    kp.ctas_per_sm = int(e->settings.sort_ctas_per_sm);
+    e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, kp, e->d_desc_sort,
+                                   e->d_ctl, spin, e->num_sms, s);
     mark(4);
     const int b = e->sorted_in_alt ? 1 : 0;
     launch_tile_ranges(e->d_keys[b], e->total_tiles, e->d_ranges, e->d_ctl, cap, e->num_sms, s);
@@ -370,7 +404,12 @@ int set_views_internal(tpd_engine* e, const tpd_view* views, uint32_t nv) {
     e->total_tiles = tiles;
     e->total_pixels = pixels;
     e->key_bits = tpd_key_bits_for_tiles(tiles);
-    e->passes = sort_pass_count(e->key_bits);
+    e->passes = sort_pass_count(e->key_bits) - 4;  // tile-id passes of the key sort
+    {
+        uint32_t vb = 0;
+        while ((1u << vb) < nv) ++vb;
+        e->depth_key_bits = 32 + vb;
+    }
     if (pixels > e->pixel_cap) {
         TPD_CUDA(e, dalloc(e->d_image, pixels * 3));
         TPD_CUDA(e, dalloc(e->d_final_T, pixels));
@@ -498,6 +537,11 @@ void tpd_destroy(tpd_engine* e) {
     dfree(e->d_image_offset);
     dfree(e->d_splats);
     dfree(e->d_offsets);
+    for (int b = 0; b < 2; ++b) {
+        dfree(e->d_dkeys[b]);
+        dfree(e->d_ditems[b]);
+    }
+    dfree(e->d_desc_depth);
     dfree(e->d_desc_pre);
     dfree(e->d_ent_mats);
     for (int b = 0; b < 2; ++b) {
@@ -836,7 +880,12 @@ int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaMemsetAsync(desc, 0, sort_desc_entries(n) * 8, s) != cudaSuccess) return TPD_ERR_DEVICE;
     launch_sort_begin(ctl, n, s);
-    const bool alt = launch_sort(keys, vals, keys_alt, vals_alt, n, key_bits, desc, ctl, kDefaultSpin, sms, s);
+    SortPlan plan;
+    plan.first_bit = 0;
+    plan.key_bits = key_bits;
+    plan.hist = ctl->sort_hist;
+    plan.hist_ready = false;
+    const bool alt = launch_sort(keys, vals, keys_alt, vals_alt, n, plan, desc, ctl, kDefaultSpin, sms, s);
     *result_in_alt = alt ? 1 : 0;
     return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;
 }

@@ -3,12 +3,15 @@
 // Reference: keygen.slang:23-53 (one thread per Gaussian looping over its tile
 // rect) and range.slang:18-35 (+ fillBuffer, GaussianEngine.cpp:843-848).
 //
-// GB300 form of keygen: a warp owns 32 consecutive Gaussians and expands their
-// keys cooperatively. Lane s of each step writes output slot s of the warp's
-// contiguous key range, finding its Gaussian by a 5-step shuffle search over
-// the warp's exclusive offsets, so stores are fully coalesced and one large
-// Gaussian no longer serialises its warp. Keys and values are bit-identical to
-// the reference's: same rect arithmetic, same row-major order, same offsets.
+// GB300 form of keygen: Gaussians are visited in depth order (a prior sort of
+// the (view | depth) keys), so the emitted keys only need a stable sort on
+// their tile-id bits afterwards: per tile the order is (depth, index), exactly
+// the reference's stable sort of (tile | depth) keys emitted in index order.
+// A warp owns 32 consecutive Gaussians and expands their keys cooperatively:
+// lane s of each step writes output slot s of the warp's contiguous key range,
+// finding its Gaussian by a 5-step shuffle search over the warp's exclusive
+// offsets, so stores are fully coalesced and one large Gaussian no longer
+// serialises its warp. Keys and values are bit-identical to the reference's.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 #include "tpd_scan.cuh"
@@ -26,48 +29,49 @@ __device__ __forceinline__ void warp_hist_add(uint32_t* sh, uint32_t d, uint32_t
     if (d != kNoDigit && lane == uint32_t(__ffs(peers) - 1)) atomicAdd(&sh[d], uint32_t(__popc(peers)));
 }
 
-// Besides the keys, builds the radix sort's digit histograms of all passes
-// (ctl->sort_hist): a Gaussian's keys share their low 32 bits (depth), so the
-// depth digits are counted once per Gaussian with its tile count as weight;
-// only the tile-id digits are counted per key.
+// Walks the (view, Gaussian) items in depth order (items[r] = v * n + i, their
+// key offsets in offsets[r]); a warp owns 32 consecutive items, whose keys are
+// contiguous. Besides the keys it counts the digits of the tile-id passes
+// (digit positions 4.. of key_bits) into ctl->sort_hist; the low 32 bits of a
+// key are its depth, already ordered, so no depth digit is counted or sorted.
 __global__ void __launch_bounds__(kKeygenThreads)
-    keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ offsets, uint32_t n,
-                  const ViewConst* __restrict__ views, uint32_t n_views, uint64_t* __restrict__ keys,
-                  uint32_t* __restrict__ vals, uint32_t capacity, uint32_t key_bits, FrameCtl* ctl) {
+    keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
+                  const uint32_t* __restrict__ offsets, uint32_t count, uint32_t n,
+                  const ViewConst* __restrict__ views, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                  uint32_t capacity, uint32_t key_bits, FrameCtl* ctl) {
     __shared__ uint32_t sh[8][256];
     const uint32_t lane = lane_id();
     const uint32_t warps_total = (gridDim.x * blockDim.x) >> 5;
     const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
-    const uint32_t wpv = (n + 31) / 32;  // warps per view; a warp never straddles a view or a 128-partition
     if (ctl->status & kStatusFatal) return;
     const uint32_t npass = min(8u, (key_bits + 7) / 8);
     for (uint32_t k = threadIdx.x; k < 8 * 256; k += blockDim.x) (&sh[0][0])[k] = 0;
     __syncthreads();
     auto digit_mask = [&](uint32_t p) { return (1u << min(8u, key_bits - 8 * p)) - 1u; };
+    const uint32_t nwarps = (count + 31) / 32;
 
-    for (uint32_t wi = warp_global; wi < wpv * n_views; wi += warps_total) {
-        const uint32_t v = wi / wpv;
-        const uint32_t g0 = (wi % wpv) * 32u;
-        const uint32_t gx = grid_x(views[v].width), gy = grid_y(views[v].height);
-        const uint32_t tile_base = views[v].tile_base;
-        const size_t vbase = size_t(v) * n;
-        const uint32_t i = g0 + lane;
-        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0, off = 0, depth_bits = 0;
-        if (i < n && TPD_INBOUNDS(ctl, 21, vbase + i, uint64_t(n) * n_views)) {
-            const float4 texel = reinterpret_cast<const float4*>(splats + vbase + i)[1];  // px, py, viewZ, radius
-            off = offsets[vbase + i];
-            if (texel.w > 0.0f) {
-                bounding_rect(texel.x, texel.y, texel.w, gx, gy, x0, y0, x1, y1);
-                depth_bits = __float_as_uint(texel.z);
+    for (uint32_t wi = warp_global; wi < nwarps; wi += warps_total) {
+        const uint32_t r = wi * 32u + lane;
+        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0, off = 0, depth_bits = 0, gi = 0, gx = 1, tile_base = 0;
+        if (r < count) {
+            const uint32_t item = items[r];
+            off = offsets[r];
+            if (TPD_INBOUNDS(ctl, 21, item, count)) {
+                const uint32_t v = item / n;
+                gi = item - v * n;
+                const ViewConst& vc = views[v];
+                gx = grid_x(vc.width);
+                tile_base = vc.tile_base;
+                const float4 texel = reinterpret_cast<const float4*>(splats + item)[1];  // px, py, viewZ, radius
+                if (texel.w > 0.0f) {
+                    bounding_rect(texel.x, texel.y, texel.w, gx, grid_y(vc.height), x0, y0, x1, y1);
+                    depth_bits = __float_as_uint(texel.z);
+                }
             }
         }
         const uint32_t w = x1 - x0;
         const uint32_t cnt = w * (y1 - y0);
-        if (cnt) {
-            for (uint32_t p = 0; p < min(npass, 4u); ++p)
-                atomicAdd(&sh[p][(depth_bits >> (8 * p)) & digit_mask(p)], cnt);
-        }
         const uint32_t incl = warp_inclusive_scan(cnt);
         const uint32_t excl = incl - cnt;
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
@@ -87,17 +91,20 @@ __global__ void __launch_bounds__(kKeygenThreads)
             const uint32_t jw = __shfl_sync(0xFFFFFFFFu, w, j);
             const uint32_t jex = __shfl_sync(0xFFFFFFFFu, excl, j);
             const uint32_t jdb = __shfl_sync(0xFFFFFFFFu, depth_bits, j);
+            const uint32_t jgi = __shfl_sync(0xFFFFFFFFu, gi, j);
+            const uint32_t jgx = __shfl_sync(0xFFFFFFFFu, gx, j);
+            const uint32_t jtb = __shfl_sync(0xFFFFFFFFu, tile_base, j);
             uint32_t tile = 0;
             const bool live = s < total;
             if (live) {
                 const uint32_t local = s - jex;
                 const uint32_t ty = jy0 + local / jw;
                 const uint32_t tx = jx0 + local % jw;
-                tile = tile_base + ty * gx + tx;
+                tile = jtb + ty * jgx + tx;
                 const uint64_t pos = uint64_t(base) + s;
-                if (pos < capacity && TPD_INBOUNDS(ctl, 20, g0 + j, n)) {
+                if (pos < capacity) {
                     keys[pos] = (uint64_t(tile) << 32) | uint64_t(jdb);
-                    vals[pos] = g0 + j;
+                    vals[pos] = jgi;
                 }
             }
             for (uint32_t p = 4; p < npass; ++p)
@@ -105,7 +112,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
         }
     }
     __syncthreads();
-    for (uint32_t p = 0; p < npass; ++p)
+    for (uint32_t p = 4; p < npass; ++p)
         for (uint32_t d = threadIdx.x; d < 256; d += blockDim.x)
             if (sh[p][d]) atomicAdd(&ctl->sort_hist[p][d], sh[p][d]);
 }
@@ -135,15 +142,15 @@ __global__ void tile_ranges_kernel(const uint64_t* __restrict__ keys, uint32_t* 
 
 }  // namespace
 
-void launch_keygen(const Splat* splats, const uint32_t* offsets, uint32_t n, const ViewConst* views,
-                   uint32_t n_views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
+void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t count, uint32_t n,
+                   const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
                    FrameCtl* ctl, int num_sms, cudaStream_t s) {
-    if (n == 0 || n_views == 0) return;
-    const uint64_t warps = uint64_t((n + 31) / 32) * n_views;
+    if (count == 0 || n == 0) return;
+    const uint64_t warps = (uint64_t(count) + 31) / 32;
     uint64_t blocks = (warps * 32 + kKeygenThreads - 1) / kKeygenThreads;
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * 8;  // persistent: bounded histogram flushes
     blocks = blocks < cap ? blocks : cap;
-    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, offsets, n, views, n_views, keys, vals,
+    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, count, n, views, keys, vals,
                                                               capacity, key_bits, ctl);
 }
 

@@ -1,5 +1,5 @@
-// preprocess.cu — kernel (a): per-Gaussian projection to a 48-byte Splat,
-// with the tile-count exclusive scan (b, first half) fused in.
+// preprocess.cu — kernel (a): per-Gaussian projection to a 48-byte Splat, the
+// depth-sort input, and the tile-count exclusive scan (b, first half).
 //
 // Reference: project.slang:33-107 with splat/common.slang (SH, frustum test,
 // camera position) and splat/volume.slang (ndc2pix, bounding rect, 3D
@@ -8,11 +8,13 @@
 // GB300 layout: a CTA of 128 threads owns 128 consecutive records (30,720 B).
 // One elected thread stages them with a single TMA bulk copy into shared
 // memory; threads then read their record with conflict-free 16-byte loads
-// (record stride 60 words). The CTA's partition id comes from an atomic
-// ticket, so the fused decoupled look-back only ever waits on CTAs that
-// started earlier. Arithmetic follows the shader source left to right with
-// matrix products accumulated k = 0..n-1; this file is compiled with
-// --fmad=false so no product is fused into an add.
+// (record stride 60 words). Besides the splat, each (view, Gaussian) gets a
+// depth-sort key (view << 32 | bits(viewZ)) whose digit histograms are
+// accumulated here. The tile counts are scanned afterwards in depth order
+// (scan_tiles_kernel<true>: gather + decoupled look-back, partitions by atomic
+// ticket). Arithmetic follows the shader source left to right with matrix
+// products accumulated k = 0..n-1; this file is compiled with --fmad=false so
+// no product is fused into an add.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 #include "tpd_scan.cuh"
@@ -62,8 +64,11 @@ __device__ __forceinline__ void mat3T(const float* A, float* B) {
 __global__ void frame_begin_kernel(FrameCtl* ctl, const float* transforms, uint32_t n_ent, const ViewConst* views,
                                    uint32_t n_views, float* ent_mats) {
     const uint32_t t = threadIdx.x;
-    for (uint32_t i = t; i < 16; i += blockDim.x) ctl->ticket[i] = 0;
-    for (uint32_t i = t; i < 8 * 256; i += blockDim.x) (&ctl->sort_hist[0][0])[i] = 0;
+    for (uint32_t i = t; i < 32; i += blockDim.x) ctl->ticket[i] = 0;
+    for (uint32_t i = t; i < 8 * 256; i += blockDim.x) {
+        (&ctl->sort_hist[0][0])[i] = 0;
+        (&ctl->depth_hist[0][0])[i] = 0;
+    }
     if (t == 0) {
         ctl->tag = ctl->tag + 1;
         ctl->status = 0;
@@ -228,25 +233,19 @@ __device__ __forceinline__ uint32_t project_one(const Rec& rec, const float* em,
     return touched;
 }
 
-// Dynamic shared memory: records (30,720 B), then per-(view, thread) tile counts.
 __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs a) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* srec = reinterpret_cast<float*>(smem_raw);
-    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(smem_raw + kPreThreads * kRecordBytes);  // [n_views][128]
+    __shared__ __align__(128) float srec[kPreThreads * kRecordFloats];
     __shared__ __align__(8) uint64_t bar;
-    __shared__ uint32_t s_part;
-    __shared__ uint32_t s_wsum[kMaxViews][kPreThreads / 32];
-    __shared__ uint32_t s_excl;
+    __shared__ uint32_t sh[8][256];  // depth-key digit counts of this CTA
 
     const uint32_t tid = threadIdx.x;
+    for (uint32_t k = tid; k < 8 * 256; k += kPreThreads) (&sh[0][0])[k] = 0;
     if (tid == 0) {
-        s_part = atomicAdd(&a.ctl->ticket[kTicketPreprocess], 1u);
         mbar_init(&bar, 1);
         fence_mbar_init();
     }
     __syncthreads();
-    const uint32_t part = s_part;
-    const uint32_t base = part * kPreThreads;
+    const uint32_t base = blockIdx.x * kPreThreads;
     const uint32_t cnt = min(kPreThreads, a.n - base);
     if (tid == 0) {
         const uint32_t bytes = cnt * kRecordBytes;  // multiple of 16 (240 = 15 x 16)
@@ -258,10 +257,10 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
 
     const uint32_t i = base + tid;
     const uint32_t e = (tid < cnt && a.ent_idx) ? a.ent_idx[i] : 0u;
-    uint32_t vis = 0;
+    const uint32_t npass = (a.depth_key_bits + 7) / 8;
     for (uint32_t v = 0; v < a.n_views; ++v) {
-        uint32_t tiles = 0;
         Splat sp;
+        uint32_t tiles = 0;
         if (tid < cnt && staged) {
             const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
             float emr[kEntityMatFloats];
@@ -273,66 +272,39 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
             sp = Splat{0.f, 0.f, 0.f, 0u, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         }
         if (tid < cnt) {
-            float4* dst = reinterpret_cast<float4*>(a.splats + size_t(v) * a.n + i);
+            const size_t item = size_t(v) * a.n + i;
+            float4* dst = reinterpret_cast<float4*>(a.splats + item);
             const float4* src = reinterpret_cast<const float4*>(&sp);
             dst[0] = src[0];
             dst[1] = src[1];
             dst[2] = src[2];
-        }
-        s_cnt[v * kPreThreads + tid] = tiles;
-        vis += tiles > 0 ? 1u : 0u;
-    }
-    if (!a.offsets) return;
-
-    // Fused exclusive scan of tile counts (prefix.slang). The sequence is
-    // ordered (partition, view, thread): within each view, Gaussians keep
-    // index order, so keys come out in the reference's emission order.
-    const uint32_t lane = tid & 31u, warp = tid >> 5;
-    for (uint32_t v = 0; v < a.n_views; ++v) {
-        const uint32_t c = s_cnt[v * kPreThreads + tid];
-        const uint32_t incl = warp_inclusive_scan(c);
-        s_cnt[v * kPreThreads + tid] = incl - c;  // exclusive prefix inside the warp
-        if (lane == 31) s_wsum[v][warp] = incl;
-    }
-    vis = warp_sum(vis);
-    __syncthreads();
-    uint32_t total = 0;
-    for (uint32_t v = 0; v < a.n_views; ++v)
-#pragma unroll
-        for (uint32_t w = 0; w < kPreThreads / 32; ++w) total += s_wsum[v][w];
-    if (warp == 0 && TPD_INBOUNDS(a.ctl, 1, part, (a.n + kPreThreads - 1) / kPreThreads)) {
-        const uint32_t ex = warp_lookback(a.desc, part, total, a.ctl->tag * 16u + 0u, &a.ctl->status, a.spin_limit,
-                                          a.never_publish != 0);
-        if (lane == 0) {
-            s_excl = ex;
-            const uint32_t nparts = (a.n + kPreThreads - 1) / kPreThreads;
-            if (part == nparts - 1) a.ctl->total_keys = ex + total;
-        }
-    }
-    if (lane == 0 && vis) atomicAdd(&a.ctl->visible, vis);
-    __syncthreads();
-    if (tid < cnt) {
-        uint32_t run = s_excl;
-        for (uint32_t v = 0; v < a.n_views; ++v) {
-            uint32_t wb = 0, vt = 0;
-#pragma unroll
-            for (uint32_t w = 0; w < kPreThreads / 32; ++w) {
-                const uint32_t sw = s_wsum[v][w];
-                if (w < warp) wb += sw;
-                vt += sw;
+            if (a.depth_keys) {
+                const uint64_t key = (uint64_t(v) << 32) | (tiles ? __float_as_uint(sp.depth) : 0xFFFFFFFFu);
+                a.depth_keys[item] = key;
+                a.depth_items[item] = uint32_t(item);
+                for (uint32_t p = 0; p < npass; ++p) {
+                    const uint32_t bits = min(8u, a.depth_key_bits - 8 * p);
+                    atomicAdd(&sh[p][uint32_t(key >> (8 * p)) & ((1u << bits) - 1u)], 1u);
+                }
             }
-            a.offsets[size_t(v) * a.n + i] = run + wb + s_cnt[v * kPreThreads + tid];
-            run += vt;
         }
     }
+    if (!a.depth_keys) return;
+    __syncthreads();
+    for (uint32_t p = 0; p < npass; ++p)
+        for (uint32_t d = tid; d < 256; d += kPreThreads)
+            if (sh[p][d]) atomicAdd(&a.ctl->depth_hist[p][d], sh[p][d]);
 }
 
-// Standalone tile-count scan: 256 threads x 4 items per partition.
+// Exclusive scan of tile counts over partitions of 256 threads x 4 items
+// (prefix.slang:40-158); kGather: counts of splats[items[r]] (depth order),
+// else of splats[r]. Total -> ctl->total_keys, non-empty count -> ctl->visible.
 constexpr uint32_t kScanThreads = 256, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
 
+template <bool kGather>
 __global__ void __launch_bounds__(kScanThreads)
-    scan_tiles_kernel(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
-                      uint32_t spin_limit, uint32_t never_publish) {
+    scan_tiles_kernel(const Splat* splats, const uint32_t* items, uint32_t n, uint32_t* offsets, uint64_t* desc,
+                      FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish) {
     __shared__ uint32_t s_part, s_excl;
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -340,14 +312,21 @@ __global__ void __launch_bounds__(kScanThreads)
     __syncthreads();
     const uint32_t part = s_part;
     const uint32_t base = part * kScanTile + tid * kScanItems;
-    uint32_t v[kScanItems], sum = 0;
+    uint32_t v[kScanItems], sum = 0, vis = 0;
 #pragma unroll
     for (uint32_t k = 0; k < kScanItems; ++k) {
-        v[k] = (base + k < n) ? splats[base + k].tiles : 0u;
+        v[k] = 0;
+        if (base + k < n) {
+            const uint32_t it = kGather ? items[base + k] : base + k;
+            v[k] = splats[it].tiles;
+        }
         sum += v[k];
+        vis += v[k] ? 1u : 0u;
     }
     const uint32_t incl = warp_inclusive_scan(sum);
     if (lane == 31) s_warp[warp] = incl;
+    vis = warp_sum(vis);
+    if (lane == 0 && vis) atomicAdd(&ctl->visible, vis);
     __syncthreads();
     uint32_t wbase = 0, total = 0;
 #pragma unroll
@@ -357,7 +336,7 @@ __global__ void __launch_bounds__(kScanThreads)
         total += sw;
     }
     if (warp == 0) {
-        const uint32_t ex = warp_lookback(desc, part, total, ctl->tag * 16u + 0u, &ctl->status, spin_limit,
+        const uint32_t ex = warp_lookback(desc, part, total, ctl->tag * 32u + kTagScan, &ctl->status, spin_limit,
                                           never_publish != 0);
         if (lane == 0) {
             s_excl = ex;
@@ -401,20 +380,23 @@ void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, 
 void launch_preprocess(const PreprocessArgs& a, cudaStream_t s) {
     if (a.n == 0 || a.n_views == 0) return;
     const uint32_t blocks = (a.n + kPreThreads - 1) / kPreThreads;
-    const size_t smem = size_t(kPreThreads) * kRecordBytes + size_t(a.n_views) * kPreThreads * 4;
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(preprocess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        configured = smem;
-    }
-    preprocess_kernel<<<blocks, kPreThreads, smem, s>>>(a);
+    preprocess_kernel<<<blocks, kPreThreads, 0, s>>>(a);
 }
 
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
                        uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
     if (n == 0) return;
     const uint32_t blocks = (n + kScanTile - 1) / kScanTile;
-    scan_tiles_kernel<<<blocks, kScanThreads, 0, s>>>(splats, n, offsets, desc, ctl, spin_limit, never_publish);
+    scan_tiles_kernel<false><<<blocks, kScanThreads, 0, s>>>(splats, nullptr, n, offsets, desc, ctl, spin_limit,
+                                                             never_publish);
+}
+
+void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t count, uint32_t* offsets, uint64_t* desc,
+                       FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
+    if (count == 0) return;
+    const uint32_t blocks = (count + kScanTile - 1) / kScanTile;
+    scan_tiles_kernel<true><<<blocks, kScanThreads, 0, s>>>(splats, items, count, offsets, desc, ctl, spin_limit,
+                                                            never_publish);
 }
 
 void launch_pack_records(const float* means, const float* log_scales, const float* quats, const float* logits,

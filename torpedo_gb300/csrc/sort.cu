@@ -75,8 +75,11 @@ __device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t
 
 __global__ void sort_begin_kernel(FrameCtl* ctl, uint32_t total) {
     const uint32_t t = threadIdx.x;
-    for (uint32_t i = t; i < 16; i += blockDim.x) ctl->ticket[i] = 0;
-    for (uint32_t i = t; i < 8 * 256; i += blockDim.x) (&ctl->sort_hist[0][0])[i] = 0;
+    for (uint32_t i = t; i < 32; i += blockDim.x) ctl->ticket[i] = 0;
+    for (uint32_t i = t; i < 8 * 256; i += blockDim.x) {
+        (&ctl->sort_hist[0][0])[i] = 0;
+        (&ctl->depth_hist[0][0])[i] = 0;
+    }
     if (t == 0) {
         ctl->tag = ctl->tag + 1;
         ctl->status = 0;
@@ -91,8 +94,8 @@ __device__ __forceinline__ void hist_add(uint32_t* h, uint32_t d) {
 }
 
 __global__ void __launch_bounds__(kHistThreads)
-    sort_histogram_kernel(const uint64_t* __restrict__ keys, uint32_t capacity, uint32_t passes, uint32_t key_bits,
-                          FrameCtl* ctl) {
+    sort_histogram_kernel(const uint64_t* __restrict__ keys, uint32_t capacity, uint32_t p0, uint32_t p1,
+                          uint32_t key_bits, uint32_t (*hist)[256], FrameCtl* ctl) {
     __shared__ uint32_t sh[8][kRadix];
     const uint32_t tid = threadIdx.x;
     for (uint32_t i = tid; i < 8 * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
@@ -114,14 +117,14 @@ __global__ void __launch_bounds__(kHistThreads)
             const uint32_t idx = base + j;
             const bool v = idx < K;
             const uint64_t k = v ? keys[idx] : 0ull;
-            for (uint32_t p = 0; p < passes; ++p)
+            for (uint32_t p = p0; p < p1; ++p)
                 hist_add(sh[p], v ? (uint32_t(k >> shift[p]) & mask[p]) : kInvalidDigit);
         }
     }
     __syncthreads();
-    for (uint32_t p = 0; p < passes; ++p)
+    for (uint32_t p = p0; p < p1; ++p)
         for (uint32_t d = tid; d < kRadix; d += kHistThreads)
-            if (sh[p][d]) atomicAdd(&ctl->sort_hist[p][d], sh[p][d]);
+            if (sh[p][d]) atomicAdd(&hist[p][d], sh[p][d]);
 }
 
 // Resolves the exclusive prefix of one digit for partition `part` by walking
@@ -166,25 +169,26 @@ template <int kMinBlocks>
 __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
     onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
-                    uint32_t pass, uint32_t shift, uint32_t bits, uint64_t* __restrict__ desc, FrameCtl* ctl,
+                    uint32_t pass, uint32_t shift, uint32_t bits, const uint32_t (*hist)[256], uint32_t ticket_slot,
+                    uint32_t tag_slot, uint32_t fixed_count, uint64_t* __restrict__ desc, FrameCtl* ctl,
                     uint32_t spin_limit) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     OnesweepSmem& S = *reinterpret_cast<OnesweepSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(ctl->total_keys, capacity);
+    const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
     const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
-    const uint32_t tag = ctl->tag * 16u + 1u + pass;
+    const uint32_t tag = ctl->tag * 32u + tag_slot;
     const uint32_t mask = (1u << bits) - 1u;
 
     // global exclusive digit offsets (histogram of this pass, scanned)
     {
-        const uint32_t h = TPD_INBOUNDS(ctl, 16, pass, 8) ? ctl->sort_hist[pass][tid] : 0u;
+        const uint32_t h = TPD_INBOUNDS(ctl, 16, pass, 8) ? hist[pass][tid] : 0u;
         const uint32_t ex = block_exclusive_scan256(h, S.wsum);
         S.gdig[tid] = ex;
     }
 
     while (true) {
-        if (tid == 0) S.part = atomicAdd(&ctl->ticket[kTicketSortBase + pass], 1u);
+        if (tid == 0) S.part = atomicAdd(&ctl->ticket[ticket_slot], 1u);
 #pragma unroll
         for (uint32_t w = 0; w < kSortWarps; ++w) S.whist[w][tid] = 0;
         __syncthreads();
@@ -308,38 +312,41 @@ size_t sort_desc_entries(uint32_t capacity) {
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s) { sort_begin_kernel<<<1, 256, 0, s>>>(ctl, total); }
 
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
-                 uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
-                 cudaStream_t s, cudaEvent_t after_hist, bool hist_ready, int ctas_per_sm) {
-    const uint32_t passes = sort_pass_count(key_bits);
-    if (passes == 0 || capacity == 0) return false;
+                 const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 cudaStream_t s) {
+    const uint32_t p0 = plan.first_bit / kRadixBits;
+    const uint32_t p1 = std::min(8u, sort_pass_count(plan.key_bits));
+    if (p1 <= p0 || capacity == 0) return false;
     const int sms = num_sms > 0 ? num_sms : 148;
     const uint32_t max_parts = (capacity + kSortTile - 1) / kSortTile;
-    if (!hist_ready) {
+    uint32_t (*hist)[256] = plan.hist ? plan.hist : ctl->sort_hist;
+    if (!plan.hist_ready) {
         const uint32_t hist_blocks = std::max(1u, std::min<uint32_t>(uint32_t(sms) * 4u, capacity / kHistChunk + 1u));
-        sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, passes, key_bits, ctl);
+        sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, p0, p1, plan.key_bits, hist, ctl);
     }
-    if (after_hist) cudaEventRecord(after_hist, s);
+    if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
     const size_t smem = sizeof(OnesweepSmem);
-    const int variant = ctas_per_sm == 3 ? 3 : 2;
+    const int variant = plan.ctas_per_sm == 3 ? 3 : 2;
     const int occ = variant == 3 ? onesweep_occupancy<3>(smem) : onesweep_occupancy<2>(smem);
     const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
     uint64_t* kin = keys;
     uint32_t* vin = vals;
     uint64_t* kout = keys_alt;
     uint32_t* vout = vals_alt;
-    for (uint32_t p = 0; p < passes; ++p) {
+    for (uint32_t p = p0; p < p1; ++p) {
         const uint32_t shift = p * kRadixBits;
-        const uint32_t bits = std::min(kRadixBits, key_bits - shift);
+        const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
+        const uint32_t ticket = plan.ticket_base + p, tag = plan.tag_base + p;
         if (variant == 3)
-            onesweep_kernel<3><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc,
-                                                                ctl, spin_limit);
+            onesweep_kernel<3><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist,
+                                                                ticket, tag, plan.fixed_count, desc, ctl, spin_limit);
         else
-            onesweep_kernel<2><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, desc,
-                                                                ctl, spin_limit);
+            onesweep_kernel<2><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist,
+                                                                ticket, tag, plan.fixed_count, desc, ctl, spin_limit);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
-    return (passes & 1u) != 0;
+    return ((p1 - p0) & 1u) != 0;
 }
 
 }  // namespace tpd

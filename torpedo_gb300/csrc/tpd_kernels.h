@@ -13,23 +13,28 @@ struct Splat;
 
 // Per-engine control block in device memory.
 struct FrameCtl {
-    uint32_t status;         // kStatus* bits, sticky until the host clears them
+    uint32_t status;         // kStatus* bits, cleared at frame start
     uint32_t tag;            // launch tag, advanced once per frame / call
     uint32_t total_keys;     // K, written by the tile-count scan
-    uint32_t visible;        // Gaussians with a non-empty tile rect
-    uint32_t ticket[16];     // partition tickets, cleared at frame start
-    uint32_t sort_hist[8][256];  // per-pass digit counts of the radix sort
-    uint32_t debug[4];       // checked builds: site, index, bound of the first failed check
-    uint32_t pad[8];
+    uint32_t visible;        // (view, Gaussian) pairs with a non-empty tile rect
+    uint32_t ticket[32];     // partition tickets, cleared at frame start
+    uint32_t sort_hist[8][256];   // digit counts of the key sort, by 8-bit digit position
+    uint32_t depth_hist[8][256];  // digit counts of the depth sort, by 8-bit digit position
+    uint32_t debug[4];       // site, index, bound of the first failed index guard
+    uint32_t pad[4];
 };
 
 // Entity matrices: rows 0..2 of view*model and rows 0..3 of projview*model.
 constexpr int kEntityMatFloats = 28;
 
-// Ticket slots.
+// Ticket slots and look-back tag slots (tag = ctl->tag * 32 + slot).
 constexpr int kTicketPreprocess = 0;
 constexpr int kTicketScan = 1;
-constexpr int kTicketSortBase = 4;  // + pass (<= 8 passes)
+constexpr int kTicketKeySortBase = 8;     // + 8-bit digit position
+constexpr int kTicketDepthSortBase = 16;  // + 8-bit digit position
+constexpr uint32_t kTagScan = 0;
+constexpr uint32_t kTagKeySort = 1;       // + digit position
+constexpr uint32_t kTagDepthSort = 16;    // + digit position
 
 struct PreprocessArgs {
     const float* recs;        // n x 60 floats (240-byte records)
@@ -42,47 +47,65 @@ struct PreprocessArgs {
     uint32_t sh_degree;
     uint32_t band3_compat;
     Splat* splats;            // n_views x n (view-major)
-    uint32_t* offsets;        // n_views x n, key offsets (fused scan); nullptr: no scan
-    uint64_t* desc;           // look-back descriptors, ceil(n/128) entries
+    // depth-sort input (nullptr: not written): item = v * n + i,
+    // key = (v << 32) | bits(viewZ), or (v << 32) | 0xFFFFFFFF when culled
+    uint64_t* depth_keys;
+    uint32_t* depth_items;
+    uint32_t depth_key_bits;  // 32 + bits of (n_views - 1); its digit histograms go to ctl->depth_hist
     FrameCtl* ctl;
-    uint32_t spin_limit;
-    uint32_t never_publish;   // test hook: partition 0 never publishes
 };
 
 constexpr uint32_t kMaxViews = 256;
 
-// Clears tickets and sort histograms of ctl and advances its tag; computes
+// Clears tickets, histograms and status of ctl and advances its tag; computes
 // entity matrices for n_views x n_ent (transforms nullptr -> identity).
 void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, const ViewConst* views,
                         uint32_t n_views, float* ent_mats, cudaStream_t s);
 void launch_preprocess(const PreprocessArgs& a, cudaStream_t s);
 
+// Tile counts of (view, Gaussian) items in depth order, gathered through
+// items[r] = v * n + i, scanned into exclusive key offsets offsets[r]; the total
+// goes to ctl->total_keys and the non-empty count to ctl->visible.
+void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t count, uint32_t* offsets, uint64_t* desc,
+                       FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s);
+
 // Standalone exclusive scan of Splat.tiles (prefix.slang); total -> ctl->total_keys.
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
                        uint32_t spin_limit, uint32_t never_publish, cudaStream_t s);
 
-// keygen.slang: keys = (tile_base + tile) << 32 | bits(viewZ), vals = Gaussian index,
-// for n_views x n (view, Gaussian) items. K is read from ctl->total_keys; keys
-// beyond capacity are dropped and flagged. Also accumulates the radix sort's
-// digit histograms for key_bits into ctl->sort_hist (cleared at frame start).
-void launch_keygen(const Splat* splats, const uint32_t* offsets, uint32_t n, const ViewConst* views,
-                   uint32_t n_views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
+// keygen.slang: keys = (tile_base + tile) << 32 | bits(viewZ), vals = Gaussian
+// index, for the items[] in depth order with their key offsets. K is read from
+// ctl->total_keys; keys beyond capacity are dropped and flagged. Also counts the
+// digits of the tile-id passes (digit positions 4.. of key_bits) into ctl->sort_hist.
+void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t count, uint32_t n,
+                   const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
                    FrameCtl* ctl, int num_sms, cudaStream_t s);
 
-// Onesweep LSD radix sort of (key, val) pairs on the low key_bits bits.
-// K = min(ctl->total_keys, capacity). Result in (keys, vals) if the pass count
-// is even, else in (keys_alt, vals_alt); returns true when it is in *_alt.
-// desc: sort_desc_entries(capacity) descriptors.
+// Onesweep LSD radix sort of (key, val) pairs on key bits [first_bit, key_bits),
+// first_bit a multiple of 8. K = min(ctl->total_keys, capacity). hist: the
+// [8][256] digit counts by digit position (hist_ready: already filled, else a
+// histogram kernel builds them); tickets ctl->ticket[ticket_base + position];
+// look-back tags ctl->tag * 32 + tag_base + position. Result in (keys, vals)
+// for an even pass count, else in (keys_alt, vals_alt); returns true for *_alt.
+// desc: sort_desc_entries(capacity) descriptors (tagged, never cleared).
 size_t sort_desc_entries(uint32_t capacity);
 uint32_t sort_pass_count(uint32_t key_bits);
-// hist_ready: ctl->sort_hist already holds the digit histograms (keygen built
-// them), so the histogram kernel is skipped. after_hist (nullable): event
-// recorded between the histogram and the first pass.
+struct SortPlan {
+    uint32_t first_bit = 0;
+    uint32_t key_bits = 64;
+    uint32_t (*hist)[256] = nullptr;
+    bool hist_ready = false;
+    uint32_t ticket_base = kTicketKeySortBase;
+    uint32_t tag_base = kTagKeySort;
+    int ctas_per_sm = 2;
+    uint32_t fixed_count = 0;          // nonzero: sort this many pairs, else min(ctl->total_keys, capacity)
+    cudaEvent_t after_hist = nullptr;  // recorded between the histogram and the first pass
+};
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
-                 uint32_t key_bits, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
-                 cudaStream_t s, cudaEvent_t after_hist = nullptr, bool hist_ready = false, int ctas_per_sm = 2);
-// Clears status, sort histograms and tickets, sets total_keys and advances the
-// tag (standalone stage calls).
+                 const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 cudaStream_t s);
+// Clears status, histograms and tickets, sets total_keys and advances the tag
+// (standalone stage calls).
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s);
 
 // range.slang: ranges[tile] = [start, end) over sorted keys, zero elsewhere.
