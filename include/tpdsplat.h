@@ -201,6 +201,20 @@ TPD_API size_t tpd_scan_workspace_size(uint32_t n);
 TPD_API int tpd_scan_tiles(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* No counterpart in the reference: tpd_scan_tiles without a workspace. The
+ * scratch is a fixed array in this library's device memory, so the call
+ * allocates nothing; it is for callers that cannot hand out device memory
+ * when they scan (all of it held by their own arena or caching allocator) or
+ * must not call cudaMalloc/cudaFree in a per-frame loop, since either can
+ * wait for the whole device. n above TPD_SCAN_STATIC_MAX_SPLATS returns
+ * TPD_ERR_CAPACITY. The first call on each device (that device current) sets
+ * up the scratch's address and should come before any stream capture. One
+ * scratch per device: calls whose work overlaps on one device race, so order
+ * them on one stream. Each call clears its scratch first; nothing has to
+ * start at zero. */
+#define TPD_SCAN_STATIC_MAX_SPLATS (1u << 24)
+TPD_API int tpd_scan_tiles_static(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total, void* stream);
+
 /* ---- host utilities (no device) ---- */
 
 /* Camera::lookAt (rendering/src/Camera.cpp:3-16) with the reference's

@@ -87,6 +87,7 @@ SIGNATURES = {
     "tpd_sort_pairs": (C.c_int, [_P, _P, _P, _P, _U32, _U32, _P, C.c_size_t, _P, C.POINTER(C.c_int)]),
     "tpd_scan_workspace_size": (C.c_size_t, [_U32]),
     "tpd_scan_tiles": (C.c_int, [_P, _U32, _P, _P, _P, C.c_size_t, _P]),
+    "tpd_scan_tiles_static": (C.c_int, [_P, _U32, _P, _P, _P]),
     "tpd_look_at": (None, [_F, _F, _F, _F]),
     "tpd_perspective": (None, [_U32, _U32, C.c_float, C.c_float, C.c_float, _F]),
     "tpd_mat4_mul": (None, [_F, _F, _F]),

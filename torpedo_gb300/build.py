@@ -30,6 +30,7 @@ SOURCES = {
     "blend.cu": [],
     "backward.cu": [],
     "engine.cu": [],
+    "scan_static.cu": [],
     "host_util.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 
