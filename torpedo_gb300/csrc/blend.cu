@@ -18,6 +18,14 @@
 //
 // power/alpha are computed by one inline function with explicit rounding
 // intrinsics, so the forward and the adjoint take identical decisions.
+//
+// Warp culling: a warp owns an 8x4 pixel block of the tile. Each staged entry
+// carries the axis-aligned box of the ellipse on which alpha >= 1/255 can hold
+// (enlarged by a relative 2e-3 and 0.01 px); a warp ballots 32 entries at a
+// time against its block and walks only the entries whose box meets it. A
+// culled pair lies outside that ellipse, where the exact alpha is below 1/255
+// and the reference skips it too. Forward and adjoint use the same blocks and
+// boxes, so they cull the same pairs.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 
@@ -41,21 +49,53 @@ struct Staged {
     float2 xy;   // px, py
     float4 q;    // qa = -0.5 log2e cx, qb = -log2e cy, qc = -0.5 log2e cz, thr
     float4 col;  // r, g, b, opacity
+    float4 box;  // x_min, x_max, y_min, y_max of the alpha >= 1/255 ellipse (empty: min > max)
 };
 
-__device__ __forceinline__ void stage_entry(const Splat* sp, float2& xy, float4& q, float4& col) {
+constexpr float kInf = __builtin_huge_valf();
+
+// Box of {d : cx dx^2 + 2 cy dx dy + cz dy^2 <= r2}, r2 = -2 ln2 thr (p2 >= thr
+// there): half-widths sqrt(r2 cz / det), sqrt(r2 cx / det), det = cx cz - cy^2
+// as a compensated difference of products (Kahan), widened for rounding.
+__device__ __forceinline__ float4 alpha_box(float x, float y, float cx, float cy, float cz, float thr) {
+    if (!(thr <= 0.0f)) return make_float4(kInf, -kInf, kInf, -kInf);  // alpha < 1/255 everywhere
+    const float w = cy * cy;
+    const float det = __fmaf_rn(cx, cz, -w) + __fmaf_rn(-cy, cy, w);
+    if (!(det > 0.0f)) return make_float4(-kInf, kInf, -kInf, kInf);  // not an ellipse: never culled
+    const float r2 = -2.0f * kLn2 * thr * (1.0f + 2e-3f);
+    const float hx = sqrtf(r2 * cz / det) + 0.01f, hy = sqrtf(r2 * cx / det) + 0.01f;
+    return make_float4(x - hx, x + hx, y - hy, y + hy);
+}
+
+__device__ __forceinline__ void stage_entry(const Splat* sp, float2& xy, float4& q, float4& col, float4& box) {
     const float4* p = reinterpret_cast<const float4*>(sp);
     const float4 c = __ldg(p + 0), tex = __ldg(p + 1), co = __ldg(p + 2);
     xy = make_float2(tex.x, tex.y);
-    const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : __int_as_float(0x7f800000);  // +inf: never blends
+    const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : kInf;  // +inf: never blends
     q = make_float4(-0.5f * kLog2e * co.x, -kLog2e * co.y, -0.5f * kLog2e * co.z, thr);
     col = make_float4(c.x, c.y, c.z, co.w);
+    box = alpha_box(tex.x, tex.y, co.x, co.y, co.z, thr);
 }
 
-__device__ __forceinline__ void stage_empty(float2& xy, float4& q, float4& col) {
+__device__ __forceinline__ void stage_empty(float2& xy, float4& q, float4& col, float4& box) {
     xy = make_float2(0.f, 0.f);
-    q = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7f800000));
+    q = make_float4(0.f, 0.f, 0.f, kInf);
     col = make_float4(0.f, 0.f, 0.f, 0.f);
+    box = make_float4(kInf, -kInf, kInf, -kInf);
+}
+
+// Pixel of thread tid within its tile, and the 8x4 block of its warp.
+__device__ __forceinline__ void warp_block_pixel(uint32_t tid, uint32_t& lx, uint32_t& ly, uint32_t& bx, uint32_t& by) {
+    const uint32_t warp = tid >> 5, lane = tid & 31u;
+    bx = 8u * (warp & 1u);
+    by = 4u * (warp >> 1);
+    lx = bx + (lane & 7u);
+    ly = by + (lane >> 3);
+}
+
+// true when entry box b meets the pixel block [x0, x0+7] x [y0, y0+3]
+__device__ __forceinline__ bool box_meets(float4 b, float x0, float y0) {
+    return b.x <= x0 + 7.0f && b.y >= x0 && b.z <= y0 + 3.0f && b.w >= y0;
 }
 
 __device__ __forceinline__ float pair_p2(float2 xy, float4 q, float pxf, float pyf, float& dx, float& dy) {
@@ -91,13 +131,18 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     __shared__ float2 s_xy[kBlendThreads];
     __shared__ float4 s_q[kBlendThreads];
     __shared__ float4 s_col[kBlendThreads];
+    __shared__ float4 s_box[kBlendThreads];
 
     const uint32_t tile = blockIdx.x;
-    if (a.ctl->status & kStatusFatal) return;
+    // an overflowed frame is re-rendered with larger key buffers; nothing to draw
+    if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
     uint32_t vi, W, H, tx, ty;
     load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
-    const uint32_t tid = threadIdx.x;
-    const uint32_t pxl = tx * kBlockX + (tid % kBlockX), pyl = ty * kBlockY + (tid / kBlockX);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    uint32_t lx, ly, bx, by;
+    warp_block_pixel(tid, lx, ly, bx, by);
+    const uint32_t pxl = tx * kBlockX + lx, pyl = ty * kBlockY + ly;
+    const float bxf = float(tx * kBlockX + bx), byf = float(ty * kBlockY + by);
     const bool inside = pxl < W && pyl < H;
     const float pxf = float(pxl), pyf = float(pyl);
     const uint32_t K = min(a.ctl->total_keys, a.capacity);
@@ -112,15 +157,22 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
         const uint32_t j = b0 + tid;
         if (j < end && TPD_INBOUNDS(a.ctl, 40, j, a.capacity)) {
             const uint32_t idx = a.vals[j];
-            if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n)) stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid]);
-            else stage_empty(s_xy[tid], s_q[tid], s_col[tid]);  // only reachable with corrupted lists
+            if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n))
+                stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);
+            else
+                stage_empty(s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);  // only reachable with corrupted lists
         }
         __syncthreads();
         const uint32_t n = min(kBlendThreads, end - b0);
         if (!TPD_INBOUNDS(a.ctl, 43, n, kBlendThreads + 1)) break;
-        if (!done) {
-#pragma unroll 4
-            for (uint32_t jj = 0; jj < n; ++jj) {
+        for (uint32_t g = 0; g < n; g += 32) {
+            if (__all_sync(0xFFFFFFFFu, done)) break;
+            const uint32_t e = g + lane;
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, e < n && box_meets(s_box[e], bxf, byf));
+            while (m) {
+                const uint32_t jj = g + uint32_t(__ffs(m) - 1);
+                m &= m - 1u;
+                if (done) continue;
                 float dx, dy;
                 const float4 q = s_q[jj];
                 const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
@@ -130,7 +182,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
                 const float tn = __fmul_rn(T, __fsub_rn(1.0f, alpha));
                 if (tn < kTMin) {
                     done = true;
-                    break;
+                    continue;
                 }
                 const float w = __fmul_rn(alpha, T);
                 C0 = __fmaf_rn(col.x, w, C0);
@@ -176,6 +228,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
     __shared__ float2 s_xy[kBlendThreads];
     __shared__ float4 s_q[kBlendThreads];
     __shared__ float4 s_col[kBlendThreads];
+    __shared__ float4 s_box[kBlendThreads];
     __shared__ uint32_t s_idx[kBlendThreads];
     __shared__ float s_acc[kBlendThreads][kG2D + 1];
 
@@ -184,7 +237,10 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
     uint32_t vi, W, H, tx, ty;
     load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
     const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    const uint32_t pxl = tx * kBlockX + (tid % kBlockX), pyl = ty * kBlockY + (tid / kBlockX);
+    uint32_t lx, ly, bx, by;
+    warp_block_pixel(tid, lx, ly, bx, by);
+    const uint32_t pxl = tx * kBlockX + lx, pyl = ty * kBlockY + ly;
+    const float bxf = float(tx * kBlockX + bx), byf = float(ty * kBlockY + by);
     const bool inside = pxl < W && pyl < H;
     const float pxf = float(pxl), pyf = float(pyl);
     const uint32_t K = min(a.ctl->total_keys, a.capacity);
@@ -222,16 +278,20 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
             const uint32_t e = uint32_t(r_end) - 1u - tid;  // descending list position (relative)
             uint32_t idx = a.vals[start + e];
             if (idx < a.n) {
-                stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid]);
+                stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);
             } else {  // only reachable with corrupted lists
                 idx = 0;
-                stage_empty(s_xy[tid], s_q[tid], s_col[tid]);
+                stage_empty(s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);
             }
             s_idx[tid] = idx;
         }
         for (uint32_t k = tid; k < kBlendThreads * (kG2D + 1); k += kBlendThreads) (&s_acc[0][0])[k] = 0.f;
         __syncthreads();
-        for (uint32_t jj = 0; jj < n; ++jj) {
+        for (uint32_t g = 0; g < n; g += 32) {
+          uint32_t m = __ballot_sync(0xFFFFFFFFu, g + lane < n && box_meets(s_box[g + lane], bxf, byf));
+          while (m) {
+            const uint32_t jj = g + uint32_t(__ffs(m) - 1);
+            m &= m - 1u;
             const uint32_t e = uint32_t(r_end) - 1u - jj;
             float gv[kG2D];
 #pragma unroll
@@ -279,6 +339,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
                     for (int k = 0; k < kG2D; ++k) atomicAdd(&s_acc[jj][k], gv[k]);
                 }
             }
+          }
         }
         __syncthreads();
         for (uint32_t k = tid; k < n * kG2D; k += kBlendThreads) {

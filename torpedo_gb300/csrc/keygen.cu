@@ -95,17 +95,17 @@ __global__ void __launch_bounds__(kKeygenThreads)
             const uint32_t jgx = __shfl_sync(0xFFFFFFFFu, gx, j);
             const uint32_t jtb = __shfl_sync(0xFFFFFFFFu, tile_base, j);
             uint32_t tile = 0;
-            const bool live = s < total;
+            // a key past the capacity is dropped and not counted, so the sort
+            // of an overflowed frame still sees a consistent histogram
+            const bool live = s < total && uint64_t(base) + s < capacity;
             if (live) {
                 const uint32_t local = s - jex;
                 const uint32_t ty = jy0 + local / jw;
                 const uint32_t tx = jx0 + local % jw;
                 tile = jtb + ty * jgx + tx;
                 const uint64_t pos = uint64_t(base) + s;
-                if (pos < capacity) {
-                    keys[pos] = (uint64_t(tile) << 32) | uint64_t(jdb);
-                    vals[pos] = jgi;
-                }
+                keys[pos] = (uint64_t(tile) << 32) | uint64_t(jdb);
+                vals[pos] = jgi;
             }
             for (uint32_t p = 4; p < npass; ++p)
                 warp_hist_add(sh[p], live ? ((tile >> (8 * (p - 4))) & digit_mask(p)) : kNoDigit, lane);

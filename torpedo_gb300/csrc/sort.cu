@@ -42,9 +42,16 @@ constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K
 constexpr uint32_t kHistThreads = 256;
 constexpr uint32_t kHistChunk = 2048;  // keys per TMA chunk (16 KB)
 
+// Reorder buffers hold one pad slot per 16 keys: digit runs of about 16 keys
+// (8-bit digits over a 4096-key partition) put the runs of consecutive digits
+// 128 B apart, which without padding lands a warp's stores on one bank when
+// its lanes carry consecutive digits (keys of one Gaussian's tile rectangle).
+constexpr uint32_t kSortTilePadded = kSortTile + kSortTile / 16;
+__device__ __forceinline__ uint32_t pad16(uint32_t i) { return i + (i >> 4); }
+
 struct OnesweepSmem {
-    uint64_t keys[kSortTile];
-    uint32_t vals[kSortTile];
+    uint64_t keys[kSortTilePadded];
+    uint32_t vals[kSortTilePadded];
     uint32_t whist[kSortWarps][kRadix];
     uint32_t gdig[kRadix];    // global exclusive digit offsets of this pass
     uint32_t lstart[kRadix];  // block-local digit start
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
             const uint32_t d = dr[i] & 511u;
             if (d < kRadix) {
                 const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-                if (TPD_INBOUNDS(ctl, 11, pos, cnt)) S.keys[pos] = k[i];
+                if (TPD_INBOUNDS(ctl, 11, pos, cnt)) S.keys[pad16(pos)] = k[i];
             }
         }
 #pragma unroll
@@ -257,7 +264,7 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
             if (d < kRadix) {
                 const uint32_t v = vals_in[base + idx];
                 const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-                if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pos] = v;
+                if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pad16(pos)] = v;
             }
         }
 
@@ -273,12 +280,12 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
 
         // coalesced write-out of digit runs
         for (uint32_t j = tid; j < cnt; j += kSortThreads) {
-            const uint64_t key = S.keys[j];
+            const uint64_t key = S.keys[pad16(j)];
             const uint32_t d = uint32_t(key >> shift) & mask;
             const uint32_t g = S.gmap[d] + j;
             if (g < capacity && TPD_INBOUNDS(ctl, 17, g, K + (K == 0))) {
                 keys_out[g] = key;
-                vals_out[g] = S.vals[j];
+                vals_out[g] = S.vals[pad16(j)];
             }
         }
         __syncthreads();  // S.keys / S.vals / S.gmap are rewritten by the next partition
