@@ -16,6 +16,13 @@ radix sort -> tile ranges -> blend, with the Gaussians resident in device memory
          all key bits, sort GB/s by the fixed formula K*(8 + 24*ceil(B/8))
   cpu_baseline  the oracle's FP32 transcription of the reference shaders (same
          4-way radix sort and pass count) on the host cores
+  fwd_bwd  training steps/s on cfg2 (200,000 Gaussians, 800x800): forward +
+         backward as one captured graph per step (tpd_step_async)
+  batched  views/s on cfg3 (500,000 Gaussians, 64 views of mixed sizes):
+         forward + backward of all 64 views as one graph per step, against
+         the plain pipeline rendering and differentiating one view per call
+  autotune  the launch setting picked for the workload (torpedo_gb300.autotune)
+         and the per-frame time of each candidate
 
 --impl reference times that CPU transcription alone (rank 0; other ranks exit).
 Launched with torchrun for N > 1: every rank renders the workload independently
@@ -213,6 +220,106 @@ def general_sort(eng, K, key_bits, stream, steps):
             "input": "the frame's keys in a seeded random order; timed with CUDA events, median"}
 
 
+def kernels_per_frame(views: int, tile_passes: int) -> int:
+    """Kernel launches of one frame: frame_begin, preprocess, depth-sort passes,
+    depth-order scan, keygen, tile-id sort passes, ranges, blend."""
+    depth_passes = math.ceil((32 + (views - 1).bit_length()) / 8)
+    return 6 + depth_passes + tile_passes
+
+
+def _params(sc, dev):
+    import numpy as np
+    import torch
+
+    return [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in
+            (sc.means, sc.log_scales, sc.quats, sc.opacity_logits, sc.sh)]
+
+
+def train_rate(cfg_name, stream, local, steps, warmup, settings):
+    """Forward + backward steps (one captured graph each) on every view of a
+    config at once; returns (ms per step, stats, views, pixels)."""
+    import torch
+
+    import torpedo_gb300 as T
+    from torpedo_gb300 import configs
+
+    dev = torch.device("cuda", local)
+    cfg = configs.CONFIGS[cfg_name]
+    sc = configs.scene(cfg)
+    cams = configs.cameras(cfg)
+    params = _params(sc, dev)
+    eng = T.GaussianEngine(device=local, stream=stream.cuda_stream, **settings)
+    try:
+        eng.compile_params(*params)
+        if len(cams) == 1:
+            eng.set_camera(cams[0])
+        else:
+            eng.set_views(cams)
+        eng.raster_frame()
+        pixels = sum(c.width * c.height for c in cams)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(int(cfg.name[3:]))
+        dimg = torch.randn(pixels * 3, generator=gen, device=dev)
+        grads = [torch.empty_like(p) for p in params]
+        eng.step_async(dimg, grads, max(3, warmup))
+        eng.sync()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.step_async(dimg, grads, steps)
+        b.record(stream)
+        st = eng.sync()
+        ms = a.elapsed_time(b) / steps
+    finally:
+        eng.close()
+    return ms, st, len(cams), pixels
+
+
+def plain_views_rate(cfg_name, local, passes, settings):
+    """The plain pipeline on the same views: per view set_camera, raster_frame
+    and backward, each call returning when its work is done (one engine per
+    image size, so no view reallocates buffers). Returns views/s."""
+    import torch
+
+    import torpedo_gb300 as T
+    from torpedo_gb300 import configs
+
+    dev = torch.device("cuda", local)
+    cfg = configs.CONFIGS[cfg_name]
+    sc = configs.scene(cfg)
+    cams = configs.cameras(cfg)
+    params = _params(sc, dev)
+    engines = {}
+    grads = [torch.empty_like(p) for p in params]
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(cfg.name[3:]))
+    dimgs = [torch.randn(c.width * c.height * 3, generator=gen, device=dev) for c in cams]
+    try:
+        for c in cams:
+            if (c.width, c.height) not in engines:
+                e = T.GaussianEngine(device=local, **settings)
+                e.compile_params(*params)
+                engines[(c.width, c.height)] = e
+
+        def one_pass():
+            for c, d in zip(cams, dimgs):
+                e = engines[(c.width, c.height)]
+                e.set_camera(c)
+                e.raster_frame()
+                e.backward(d, *grads)
+
+        one_pass()  # warm-up: sizes the key buffers of every engine
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(passes):
+            one_pass()
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t0
+    finally:
+        for e in engines.values():
+            e.close()
+    return passes * len(cams) / dt
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -236,11 +343,22 @@ def run_ours(args):
     sc = configs.scene(cfg)
     cam = configs.cameras(cfg)[0]
 
-    eng = T.GaussianEngine(device=local, stream=stream.cuda_stream, sort_ctas_per_sm=args.sort_ctas)
-    eng.compile(sc.records)
-    eng.set_camera(cam)
+    def make_engine(settings, stage_timing=False):
+        e = T.GaussianEngine(device=local, stream=stream.cuda_stream, stage_timing=stage_timing, **settings)
+        e.compile(sc.records)
+        e.set_camera(cam)
+        e.raster_frame()
+        return e
+
+    if args.sort_ctas:
+        settings, tuned = {"sort_ctas_per_sm": args.sort_ctas}, None
+    else:
+        from torpedo_gb300 import autotune
+
+        settings, tuned = autotune.tune(make_engine, lambda e, k: e.raster_frames_async(k), stream)
+    eng = make_engine(settings)
     st = eng.raster_frame()
-    kernels_per_frame = 3 + 1 + 1 + st["sort_passes"] + 1 + 1  # begin, preprocess, keygen, hist, passes, ranges, blend
+    launches_per_frame = kernels_per_frame(1, int(st["sort_passes"]))
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -275,11 +393,7 @@ def run_ours(args):
     value = world * args.steps / (ms / 1000.0)
 
     # stage-timed region: live per-stage durations for the roofline
-    eng_t = T.GaussianEngine(device=local, stream=stream.cuda_stream, stage_timing=True,
-                             sort_ctas_per_sm=args.sort_ctas)
-    eng_t.compile(sc.records)
-    eng_t.set_camera(cam)
-    eng_t.raster_frame()
+    eng_t = make_engine(settings, stage_timing=True)
     eng_t.stage_times(reset=True)
     barrier()
     eng_t.raster_frames_async(args.steps)
@@ -318,6 +432,24 @@ def run_ours(args):
         t = json.loads(tfile.read_text())
         traffic = int(t["dram_bytes_per_key"] * K)
     general = general_sort(eng, K, key_bits, stream, args.steps) if not args.no_general_sort else None
+    eng.close()
+
+    fwd_bwd = batched = None
+    if not args.no_train:
+        ms2, st2, _, _ = train_rate("cfg2", stream, local, 50, 3, settings)
+        fwd_bwd = {"config": "cfg2: 200,000 Gaussians (means N(0,1)^3), one 800x800 view, dL/dimage ~ N(0,1)",
+                   "value": round(1000.0 / ms2, 3), "unit": "it/s", "ms_per_step": round(ms2, 4),
+                   "keys": int(st2["keys"]),
+                   "step": "forward frame + backward to means, log-scales, quaternions, opacity logits, SH; "
+                           "one captured CUDA graph per step"}
+        ms3, st3, views3, pixels3 = train_rate("cfg3", stream, local, 5, 2, settings)
+        plain = plain_views_rate("cfg3", local, 1, settings)
+        batched = {"config": "cfg3: 500,000 Gaussians (means N(0,1)^3), 64 views on a sphere of radius 5, sizes "
+                             "from {640x480, 1280x720, 1920x1080} (seed 3), dL/dimage ~ N(0,1)",
+                   "views_per_s": round(views3 * 1000.0 / ms3, 2), "ms_per_step": round(ms3, 3),
+                   "keys": int(st3["keys"]), "pixels": pixels3,
+                   "plain_views_per_s": round(plain, 2), "batched_over_plain": round(views3 * 1000.0 / ms3 / plain, 3),
+                   "plain": "one view per call: set_camera, raster_frame, backward, each waiting for its work"}
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -333,8 +465,11 @@ def run_ours(args):
                        "note": "Gaussians sorted by depth first (N items), then the K keys on their tile-id bits only"},
         "general_sort": general,
         "stages_ms": {k: round(v, 4) for k, v in stage_avg.items()},
-        "gpu_launches": kernels_per_frame * args.steps,
+        "gpu_launches": launches_per_frame * args.steps,
         "clocks": clk,
+        "autotune": {"settings": settings, "ms_per_frame": tuned},
+        "fwd_bwd": fwd_bwd,
+        "batched": batched,
     }
     if e2e:
         line["e2e"] = e2e
@@ -345,7 +480,6 @@ def run_ours(args):
                                 "kind": "port",
                                 "sample": f"{len(times)} whole frames of the FP32 transcription of the reference "
                                           f"shaders (4-way radix sort), K={k}"}
-    eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -362,7 +496,9 @@ def main():
     ap.add_argument("--cpu-baseline-s", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-general-sort", action="store_true")
-    ap.add_argument("--sort-ctas", type=int, default=2, help="radix pass kernel residency (2 or 3 CTAs per SM)")
+    ap.add_argument("--sort-ctas", type=int, default=0,
+                    help="radix pass kernel residency (2 or 3 CTAs per SM); 0 = autotune")
+    ap.add_argument("--no-train", action="store_true", help="skip the cfg2 and cfg3 forward+backward measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -174,6 +174,16 @@ TPD_API int tpd_read_image(tpd_engine* e, void* dst, uint32_t format, int dst_is
 TPD_API int tpd_backward(tpd_engine* e, const float* dL_dimage, float* g_means, float* g_log_scales, float* g_quats,
                  float* g_logits, float* g_sh);
 
+/* Training step, no counterpart in the reference (it has no backward): count
+ * times forward frame + backward on the current views, enqueued without host
+ * waits; with use_graph both are one captured CUDA graph per step (captured
+ * again when the pointers change). Gradients are overwritten each step.
+ * Needs a frame rendered with tpd_raster_frame after any change (it sizes the
+ * key buffers); tpd_sync then reports TPD_ERR_CAPACITY if the keys outgrew
+ * them. */
+TPD_API int tpd_step_async(tpd_engine* e, const float* dL_dimage, float* g_means, float* g_log_scales, float* g_quats,
+                   float* g_logits, float* g_sh, uint32_t count);
+
 TPD_API int tpd_get_buffer(const tpd_engine* e, uint32_t which, void** device_ptr, uint64_t* bytes);
 /* Copies bytes [offset, offset + bytes) of an internal buffer (TPD_BUF_*) to dst. */
 TPD_API int tpd_read_buffer(tpd_engine* e, uint32_t which, void* dst, uint64_t offset, uint64_t bytes,

@@ -103,3 +103,36 @@ def test_autograd_function(cuda):
         torch.testing.assert_close(a.grad, b, rtol=1e-4, atol=1e-6)
     eng.close()
     eng2.close()
+
+
+@pytest.mark.parametrize("views", [1, 3])
+def test_step_async_graph_matches_backward(cuda, views):
+    """tpd_step_async (forward + backward captured as one graph per step) gives
+    the gradients of tpd_raster_frame + tpd_backward on the same views; the
+    adjoint sums with float atomics, so the bar is 1e-5 relative."""
+    torch = cuda
+    sc = configs.scene("cfg2", 20_000)
+    eyes = configs.fibonacci_sphere(views)
+    sizes = [(96, 80), (64, 64), (120, 72)]
+    cams = [T.Camera.orbit(tuple(float(x) for x in eyes[v]), *sizes[v % 3]) for v in range(views)]
+    dev = torch.device("cuda")
+    params = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in
+              (sc.means, sc.log_scales, sc.quats, sc.opacity_logits, sc.sh)]
+    pixels = sum(c.width * c.height for c in cams)
+    dimg = torch.from_numpy(np.random.default_rng(5).normal(size=pixels * 3).astype(np.float32)).to(dev)
+    eng = T.GaussianEngine(use_graph=True)
+    eng.compile_params(*params)
+    if views == 1:
+        eng.set_camera(cams[0])
+    else:
+        eng.set_views(cams)
+    eng.raster_frame()
+    ref = [t.cpu().numpy() for t in eng.backward(dimg)]
+    grads = [torch.full_like(p, float("nan")) for p in params]
+    eng.step_async(dimg, grads, count=3)
+    eng.sync()
+    eng.close()
+    for name, a, b in zip(NAMES, [g.cpu().numpy() for g in grads], ref):
+        nb = np.linalg.norm(b)
+        assert np.all(np.isfinite(a)), name
+        assert np.linalg.norm(a - b) <= 1e-5 * nb + 1e-12, (name, np.linalg.norm(a - b) / max(nb, 1e-30))

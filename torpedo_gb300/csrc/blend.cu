@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
     __shared__ float s_acc[kBlendThreads][kG2D + 1];
 
     const uint32_t tile = blockIdx.x;
-    if (a.ctl->status & kStatusFatal) return;
+    if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
     uint32_t vi, W, H, tx, ty;
     load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
     const uint32_t tid = threadIdx.x, lane = tid & 31u;

@@ -122,6 +122,10 @@ struct tpd_engine {
     bool graph_valid = false;
     bool needs_eager = true;  // the first frame after any change runs without a graph
     uint64_t frames = 0;
+
+    // forward + backward step graph (tpd_step_async), keyed by the caller's pointers
+    cudaGraphExec_t step_graph = nullptr;
+    const void* step_key[6] = {};
 };
 
 namespace {
@@ -148,11 +152,18 @@ cudaError_t dalloc(T*& p, uint64_t count) {
     return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
 }
 
+void invalidate_step_graph(tpd_engine* e) {
+    if (e->step_graph) cudaGraphExecDestroy(e->step_graph);
+    e->step_graph = nullptr;
+    for (auto& k : e->step_key) k = nullptr;
+}
+
 void invalidate_graph(tpd_engine* e) {
     if (e->graph) cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;
     e->graph_valid = false;
     e->needs_eager = true;
+    invalidate_step_graph(e);
 }
 
 // Views x n sized buffers.
@@ -755,29 +766,42 @@ int tpd_read_image(tpd_engine* e, void* dst, uint32_t format, int dst_is_device)
     return wait_stream(e);
 }
 
-int tpd_backward(tpd_engine* e, const float* dL_dimage, float* g_means, float* g_log_scales, float* g_quats,
-                 float* g_logits, float* g_sh) {
-    if (!e || !dL_dimage) return TPD_ERR_ARG;
-    if (!e->frame_valid) return fail(e, TPD_ERR_STATE, "backward before a rendered frame");
-    cudaSetDevice(e->device);
+}  // extern "C"
+
+namespace {
+
+struct BackwardOut {
+    float *means, *log_scales, *quats, *logits, *sh;
+};
+
+// Sizes the backward's buffers (before any capture: this may allocate) and
+// points absent gradient outputs at engine scratch.
+int prepare_backward(tpd_engine* e, BackwardOut& o) {
     const uint64_t g2d = uint64_t(e->n) * e->n_views * 9;
     if (g2d > e->g2d_cap) {
+        invalidate_step_graph(e);
         TPD_CUDA(e, dalloc(e->d_g2d, g2d));
         e->g2d_cap = g2d;
     }
     const uint64_t gs = uint64_t(e->n) * (3 + 3 + 4 + 1 + 48);
-    if ((!g_means || !g_log_scales || !g_quats || !g_logits || !g_sh) && gs > e->gscratch_cap) {
+    if ((!o.means || !o.log_scales || !o.quats || !o.logits || !o.sh) && gs > e->gscratch_cap) {
+        invalidate_step_graph(e);
         TPD_CUDA(e, dalloc(e->d_gscratch, gs));
         e->gscratch_cap = gs;
     }
     float* sc = e->d_gscratch;
     const uint64_t n = e->n;
-    if (!g_means) g_means = sc;
-    if (!g_log_scales) g_log_scales = sc + n * 3;
-    if (!g_quats) g_quats = sc + n * 6;
-    if (!g_logits) g_logits = sc + n * 10;
-    if (!g_sh) g_sh = sc + n * 11;
-    TPD_CUDA(e, cudaMemsetAsync(e->d_g2d, 0, g2d * 4, e->stream));
+    if (!o.means) o.means = sc;
+    if (!o.log_scales) o.log_scales = sc + n * 3;
+    if (!o.quats) o.quats = sc + n * 6;
+    if (!o.logits) o.logits = sc + n * 10;
+    if (!o.sh) o.sh = sc + n * 11;
+    return TPD_OK;
+}
+
+// Blend adjoint (per-splat gradients, zeroed first) then preprocess adjoint.
+void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& o) {
+    cudaMemsetAsync(e->d_g2d, 0, uint64_t(e->n) * e->n_views * 9 * 4, e->stream);
     const int b = e->sorted_in_alt ? 1 : 0;
     BlendBackwardArgs bb{};
     bb.splats = e->d_splats;
@@ -809,14 +833,67 @@ int tpd_backward(tpd_engine* e, const float* dL_dimage, float* g_means, float* g
     pb.band3_compat = e->settings.band3_compat;
     pb.splats = e->d_splats;
     pb.g2d = e->d_g2d;
-    pb.g_means = g_means;
-    pb.g_log_scales = g_log_scales;
-    pb.g_quats = g_quats;
-    pb.g_logits = g_logits;
-    pb.g_sh = g_sh;
+    pb.g_means = o.means;
+    pb.g_log_scales = o.log_scales;
+    pb.g_quats = o.quats;
+    pb.g_logits = o.logits;
+    pb.g_sh = o.sh;
     launch_preprocess_backward(pb, e->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tpd_backward(tpd_engine* e, const float* dL_dimage, float* g_means, float* g_log_scales, float* g_quats,
+                 float* g_logits, float* g_sh) {
+    if (!e || !dL_dimage) return TPD_ERR_ARG;
+    if (!e->frame_valid) return fail(e, TPD_ERR_STATE, "backward before a rendered frame");
+    cudaSetDevice(e->device);
+    BackwardOut o{g_means, g_log_scales, g_quats, g_logits, g_sh};
+    const int rc = prepare_backward(e, o);
+    if (rc != TPD_OK) return rc;
+    enqueue_backward(e, dL_dimage, o);
     TPD_CUDA(e, cudaGetLastError());
     return wait_stream(e);
+}
+
+int tpd_step_async(tpd_engine* e, const float* dL_dimage, float* g_means, float* g_log_scales, float* g_quats,
+                   float* g_logits, float* g_sh, uint32_t count) {
+    if (!e || !dL_dimage) return TPD_ERR_ARG;
+    if (!e->frame_valid || e->needs_eager)
+        return fail(e, TPD_ERR_STATE, "render one frame with tpd_raster_frame after any change first");
+    cudaSetDevice(e->device);
+    BackwardOut o{g_means, g_log_scales, g_quats, g_logits, g_sh};
+    const int rc = prepare_backward(e, o);
+    if (rc != TPD_OK) return rc;
+    const bool graph = e->settings.use_graph && !e->settings.stage_timing;
+    const void* key[6] = {dL_dimage, o.means, o.log_scales, o.quats, o.logits, o.sh};
+    if (graph && (!e->step_graph || std::memcmp(key, e->step_key, sizeof(key)) != 0)) {
+        invalidate_step_graph(e);
+        cudaGraph_t g = nullptr;
+        TPD_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_frame(e);
+        enqueue_backward(e, dL_dimage, o);
+        TPD_CUDA(e, cudaStreamEndCapture(e->stream, &g));
+        cudaGraphExec_t ge = nullptr;
+        const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        TPD_CUDA(e, err);
+        e->step_graph = ge;
+        std::memcpy(e->step_key, key, sizeof(key));
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        if (graph) {
+            TPD_CUDA(e, cudaGraphLaunch(e->step_graph, e->stream));
+        } else {
+            enqueue_frame(e);
+            enqueue_backward(e, dL_dimage, o);
+        }
+    }
+    TPD_CUDA(e, cudaGetLastError());
+    e->frames += count;
+    return TPD_OK;
 }
 
 int tpd_get_buffer(const tpd_engine* e, uint32_t which, void** ptr, uint64_t* bytes) {

@@ -310,6 +310,18 @@ class GaussianEngine:
                                      g_quats.data_ptr(), g_logits.data_ptr(), g_sh.data_ptr()), self._h)
         return g_means, g_log_scales, g_quats, g_logits, g_sh
 
+    def step_async(self, dL_dimage, grads, count: int = 1):
+        """count training steps (forward frame + backward) enqueued on the engine's
+        stream without host waits; grads = (g_means, g_log_scales, g_quats,
+        g_logits, g_sh) CUDA tensors, overwritten each step. Call sync() to wait."""
+        import torch
+
+        dimg = dL_dimage.contiguous()
+        ptrs = [g.data_ptr() for g in grads]
+        torch.cuda.current_stream(dimg.device).synchronize()  # inputs written on torch's stream
+        _check(L.load().tpd_step_async(self._h, dimg.data_ptr(), *ptrs, count), self._h)
+        self._step_refs = (dimg, tuple(grads))  # kept alive while the steps run
+
 
 def sort_pairs(keys, vals, key_bits: int):
     """Stable radix sort of CUDA tensors keys (int64 holding u64) / vals (int32 holding u32) on the low key_bits."""
