@@ -117,7 +117,7 @@ enum {
     TPD_BUF_IMAGE = 6,     /* pixels x 3 floats, views packed */
     TPD_BUF_FINAL_T = 7,   /* pixels floats */
     TPD_BUF_N_CONTRIB = 8, /* pixels u32 */
-    TPD_BUF_G2D = 9        /* views x n x 9 floats after tpd_backward */
+    TPD_BUF_G2D = 9        /* views x n x 12 floats after tpd_backward: px, py, conic xyz, opacity, rgb, 3 pad */
 };
 
 TPD_API const char* tpd_version(void);

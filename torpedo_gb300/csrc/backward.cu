@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(PreprocessBack
     for (uint32_t v = 0; v < a.n_views; ++v) {
         const Splat& sp = a.splats[size_t(v) * a.n + i];
         if (!(sp.radius > 0.0f)) continue;
-        const float* g = a.g2d + (size_t(v) * a.n + i) * 9;
+        const float* g = a.g2d + (size_t(v) * a.n + i) * kG2DStride;
         const ViewConst& vc = a.views[v];
         const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
         float vp[3], cp[4];

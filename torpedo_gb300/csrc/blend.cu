@@ -224,13 +224,41 @@ __device__ __forceinline__ float warp_red(float v) {
 
 constexpr int kG2D = 9;  // px, py, conic.x, conic.y, conic.z, opacity, r, g, b
 
+// Sums v[0..7] over the warp with a transposed butterfly: each of the first
+// three exchanges halves the values a lane holds, the last two add single
+// values. Afterwards lane 4j holds the warp sum of v[j] (j = 0..7).
+__device__ __forceinline__ float warp_sum8_transposed(const float (&v)[8], uint32_t lane) {
+    float a[4], b[2], c;
+    const bool u4 = (lane >> 4) & 1u, u3 = (lane >> 3) & 1u, u2 = (lane >> 2) & 1u;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float send = u4 ? v[i] : v[i + 4];
+        const float keep = u4 ? v[i + 4] : v[i];
+        a[i] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 16);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const float send = u3 ? a[i] : a[i + 2];
+        const float keep = u3 ? a[i + 2] : a[i];
+        b[i] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 8);
+    }
+    {
+        const float send = u2 ? b[0] : b[1];
+        const float keep = u2 ? b[1] : b[0];
+        c = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 4);
+    }
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 2);
+    c += __shfl_xor_sync(0xFFFFFFFFu, c, 1);
+    return c;
+}
+
 __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBackwardArgs a) {
     __shared__ float2 s_xy[kBlendThreads];
     __shared__ float4 s_q[kBlendThreads];
     __shared__ float4 s_col[kBlendThreads];
     __shared__ float4 s_box[kBlendThreads];
     __shared__ uint32_t s_idx[kBlendThreads];
-    __shared__ float s_acc[kBlendThreads][kG2D + 1];
+    __shared__ __align__(16) float s_acc[kBlendThreads][kG2DStride];
 
     const uint32_t tile = blockIdx.x;
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
@@ -285,67 +313,70 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
             }
             s_idx[tid] = idx;
         }
-        for (uint32_t k = tid; k < kBlendThreads * (kG2D + 1); k += kBlendThreads) (&s_acc[0][0])[k] = 0.f;
+        for (uint32_t k = tid; k < kBlendThreads * kG2DStride; k += kBlendThreads) (&s_acc[0][0])[k] = 0.f;
         __syncthreads();
         for (uint32_t g = 0; g < n; g += 32) {
-          uint32_t m = __ballot_sync(0xFFFFFFFFu, g + lane < n && box_meets(s_box[g + lane], bxf, byf));
-          while (m) {
-            const uint32_t jj = g + uint32_t(__ffs(m) - 1);
-            m &= m - 1u;
-            const uint32_t e = uint32_t(r_end) - 1u - jj;
-            float gv[kG2D];
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, g + lane < n && box_meets(s_box[g + lane], bxf, byf));
+            while (m) {
+                const uint32_t jj = g + uint32_t(__ffs(m) - 1);
+                m &= m - 1u;
+                const uint32_t e = uint32_t(r_end) - 1u - jj;
+                float gv[kG2D];
 #pragma unroll
-            for (int k = 0; k < kG2D; ++k) gv[k] = 0.f;
-            bool contrib = false;
-            if (inside && e < last) {
-                float dx, dy;
-                const float4 q = s_q[jj];
-                const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
-                if (!pair_skipped(p2, q.w)) {
-                    const float4 col = s_col[jj];
-                    const float G = ex2_approx(p2);
-                    const float raw = __fmul_rn(col.w, G);
-                    const float alpha = fminf(kAlphaMax, raw);
-                    contrib = true;
-                    const float one_m = 1.0f - alpha;
-                    const float Tb = T / one_m;  // transmittance in front of this entry
-                    const float w = alpha * Tb;
-                    gv[6] = g0 * w;
-                    gv[7] = g1 * w;
-                    gv[8] = g2 * w;
-                    const float dA = g0 * (col.x * Tb - S0 / one_m) + g1 * (col.y * Tb - S1 / one_m) +
-                                     g2 * (col.z * Tb - S2 / one_m);
-                    S0 = fmaf(col.x, w, S0);
-                    S1 = fmaf(col.y, w, S1);
-                    S2 = fmaf(col.z, w, S2);
-                    T = Tb;
-                    if (raw <= kAlphaMax) {
-                        // power = p2 ln2; d power / d(dx, dy) = ln2 (2 qa dx + qb dy, 2 qc dy + qb dx)
-                        const float dpow = dA * alpha;
-                        gv[5] = dA * G;
-                        gv[0] = dpow * kLn2 * (2.0f * q.x * dx + q.y * dy);
-                        gv[1] = dpow * kLn2 * (2.0f * q.z * dy + q.y * dx);
-                        gv[2] = dpow * (-0.5f * dx * dx);
-                        gv[3] = dpow * (-dx * dy);
-                        gv[4] = dpow * (-0.5f * dy * dy);
+                for (int k = 0; k < kG2D; ++k) gv[k] = 0.f;
+                bool contrib = false;
+                if (inside && e < last) {
+                    float dx, dy;
+                    const float4 q = s_q[jj];
+                    const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
+                    if (!pair_skipped(p2, q.w)) {
+                        const float4 col = s_col[jj];
+                        const float G = ex2_approx(p2);
+                        const float raw = __fmul_rn(col.w, G);
+                        const float alpha = fminf(kAlphaMax, raw);
+                        contrib = true;
+                        const float inv = __frcp_rn(1.0f - alpha);
+                        const float Tb = T * inv;  // transmittance in front of this entry
+                        const float w = alpha * Tb;
+                        gv[6] = g0 * w;
+                        gv[7] = g1 * w;
+                        gv[8] = g2 * w;
+                        const float dA = g0 * (col.x * Tb - S0 * inv) + g1 * (col.y * Tb - S1 * inv) +
+                                         g2 * (col.z * Tb - S2 * inv);
+                        S0 = fmaf(col.x, w, S0);
+                        S1 = fmaf(col.y, w, S1);
+                        S2 = fmaf(col.z, w, S2);
+                        T = Tb;
+                        if (raw <= kAlphaMax) {
+                            // power = p2 ln2; d power / d(dx, dy) = ln2 (2 qa dx + qb dy, 2 qc dy + qb dx)
+                            const float dpow = dA * alpha;
+                            gv[5] = dA * G;
+                            gv[0] = dpow * kLn2 * (2.0f * q.x * dx + q.y * dy);
+                            gv[1] = dpow * kLn2 * (2.0f * q.z * dy + q.y * dx);
+                            gv[2] = dpow * (-0.5f * dx * dx);
+                            gv[3] = dpow * (-dx * dy);
+                            gv[4] = dpow * (-0.5f * dy * dy);
+                        }
                     }
                 }
-            }
-            if (__any_sync(0xFFFFFFFFu, contrib)) {
+                if (__any_sync(0xFFFFFFFFu, contrib)) {
+                    const float lo[8] = {gv[0], gv[1], gv[2], gv[3], gv[4], gv[5], gv[6], gv[7]};
+                    const float r = warp_sum8_transposed(lo, lane);
+                    float b = gv[8];
 #pragma unroll
-                for (int k = 0; k < kG2D; ++k) gv[k] = warp_red(gv[k]);
-                if (lane == 0) {
-#pragma unroll
-                    for (int k = 0; k < kG2D; ++k) atomicAdd(&s_acc[jj][k], gv[k]);
+                    for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
+                    if ((lane & 3u) == 0) atomicAdd(&s_acc[jj][lane >> 2], r);
+                    if (lane == 0) atomicAdd(&s_acc[jj][8], b);
                 }
             }
-          }
         }
         __syncthreads();
-        for (uint32_t k = tid; k < n * kG2D; k += kBlendThreads) {
-            const uint32_t jj = k / kG2D, f = k % kG2D;
-            const float v = s_acc[jj][f];
-            if (v != 0.0f) atomicAdd(g2d_view + size_t(s_idx[jj]) * a.g2d_stride + f, v);
+        // one 16-byte vector atomic per non-zero quarter of an entry's record
+        for (uint32_t k = tid; k < n * 3; k += kBlendThreads) {
+            const uint32_t jj = k / 3, c = k % 3;
+            const float4 v = reinterpret_cast<const float4*>(&s_acc[jj][0])[c];
+            if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f)
+                atomicAdd(reinterpret_cast<float4*>(g2d_view + size_t(s_idx[jj]) * kG2DStride) + c, v);
         }
     }
 }

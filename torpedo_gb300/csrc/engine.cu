@@ -777,7 +777,7 @@ struct BackwardOut {
 // Sizes the backward's buffers (before any capture: this may allocate) and
 // points absent gradient outputs at engine scratch.
 int prepare_backward(tpd_engine* e, BackwardOut& o) {
-    const uint64_t g2d = uint64_t(e->n) * e->n_views * 9;
+    const uint64_t g2d = uint64_t(e->n) * e->n_views * kG2DStride;
     if (g2d > e->g2d_cap) {
         invalidate_step_graph(e);
         TPD_CUDA(e, dalloc(e->d_g2d, g2d));
@@ -801,7 +801,7 @@ int prepare_backward(tpd_engine* e, BackwardOut& o) {
 
 // Blend adjoint (per-splat gradients, zeroed first) then preprocess adjoint.
 void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& o) {
-    cudaMemsetAsync(e->d_g2d, 0, uint64_t(e->n) * e->n_views * 9 * 4, e->stream);
+    cudaMemsetAsync(e->d_g2d, 0, uint64_t(e->n) * e->n_views * kG2DStride * 4, e->stream);
     const int b = e->sorted_in_alt ? 1 : 0;
     BlendBackwardArgs bb{};
     bb.splats = e->d_splats;
@@ -818,8 +818,7 @@ void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& 
     bb.n_contrib = e->d_n_contrib;
     bb.dL_dimage = dL_dimage;
     bb.g2d = e->d_g2d;
-    bb.g2d_stride = 9;
-    bb.g2d_view_stride = uint64_t(e->n) * 9;
+    bb.g2d_view_stride = uint64_t(e->n) * kG2DStride;
     launch_blend_backward(bb, e->stream);
     PreprocessBackwardArgs pb{};
     pb.recs = e->d_recs;
@@ -912,7 +911,7 @@ int tpd_get_buffer(const tpd_engine* e, uint32_t which, void** ptr, uint64_t* by
         case TPD_BUF_IMAGE: p = e->d_image; sz = e->total_pixels * 12; break;
         case TPD_BUF_FINAL_T: p = e->d_final_T; sz = e->total_pixels * 4; break;
         case TPD_BUF_N_CONTRIB: p = e->d_n_contrib; sz = e->total_pixels * 4; break;
-        case TPD_BUF_G2D: p = e->d_g2d; sz = vn * 9 * 4; break;
+        case TPD_BUF_G2D: p = e->d_g2d; sz = vn * kG2DStride * 4; break;
         default: return TPD_ERR_ARG;
     }
     *ptr = p;

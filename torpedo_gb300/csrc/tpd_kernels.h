@@ -147,11 +147,14 @@ struct BlendBackwardArgs {
     const float* final_T;
     const uint32_t* n_contrib;
     const float* dL_dimage;   // HWC float3
-    float* g2d;               // n x 9 (px, py, conic.xyz, opacity, rgb), accumulated
-    uint32_t g2d_stride;      // floats between consecutive Gaussians' g2d (9) ...
-    uint64_t g2d_view_stride; // ... and between views (batched: n*9; single: 0)
+    float* g2d;               // n x kG2DStride (px, py, conic.xyz, opacity, rgb, 3 pad), accumulated
+    uint64_t g2d_view_stride; // floats between views' g2d (n * kG2DStride)
 };
 void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s);
+
+// Per-splat gradient record of the blend adjoint: 9 used floats padded to 12
+// (48 B), so it is accumulated with three 16-byte vector atomics.
+constexpr uint32_t kG2DStride = 12;
 
 struct PreprocessBackwardArgs {
     const float* recs;
@@ -164,7 +167,7 @@ struct PreprocessBackwardArgs {
     uint32_t sh_degree;
     uint32_t band3_compat;
     const Splat* splats;      // per view n splats, view-major
-    const float* g2d;         // per view n x 9, view-major
+    const float* g2d;         // per view n x kG2DStride, view-major
     float* g_means;           // n x 3
     float* g_log_scales;      // n x 3
     float* g_quats;           // n x 4
