@@ -47,6 +47,7 @@ def load():
             "orc_tile_ranges": (None, [P, C.c_uint64, C.c_uint32, P]),
             "orc_blend_f32": (None, [P, P, P, C.c_uint32, C.c_uint32, P, P, P, C.c_int]),
             "orc_blend_f64": (None, [P, P, P, C.c_uint32, C.c_uint32, P, P, P, P]),
+            "orc_blend_pair_count": (None, [P, P, P, C.c_uint32, C.c_uint32, P, P, C.c_int]),
             "orc_frame_f32": (C.c_uint64, [P, C.c_uint32, C.POINTER(OrcCamera), C.c_uint32, P, C.c_int, C.c_uint32]),
             "orc_render_params_f64": (None, [C.POINTER(OrcParams64), C.c_uint32, C.POINTER(OrcCamera), C.c_uint32,
                                              C.c_int, P, P, P]),
@@ -157,6 +158,17 @@ def blend_f32(splats_u32, vals, ranges, width, height, threads=0):
     load().orc_blend_f32(s.ctypes.data, v.ctypes.data if v.size else None, r.ctypes.data, width, height,
                          img.ctypes.data, T.ctypes.data, nc.ctypes.data, threads)
     return img, T, nc
+
+
+def blend_pair_count(splats_u32, vals, ranges, width, height, threads=0):
+    """(evaluated, contributing) (pixel, entry) pairs of the FP32 blend's rules."""
+    s = _c(splats_u32, np.uint32)
+    v = _c(vals, np.uint32)
+    r = _c(ranges, np.uint32)
+    ev, co = C.c_uint64(0), C.c_uint64(0)
+    load().orc_blend_pair_count(s.ctypes.data, v.ctypes.data if v.size else None, r.ctypes.data, width, height,
+                                C.byref(ev), C.byref(co), threads)
+    return int(ev.value), int(co.value)
 
 
 def blend_f64(splat64, vals, ranges, width, height):

@@ -511,6 +511,45 @@ void orc_blend_f32(const uint32_t* splats, const uint32_t* vals, const uint32_t*
     }
 }
 
+void orc_blend_pair_count(const uint32_t* splats, const uint32_t* vals, const uint32_t* ranges,
+                          uint32_t width, uint32_t height, uint64_t* evaluated, uint64_t* contributing,
+                          int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    const uint32_t gx = (width + BLOCK - 1) / BLOCK, gy = (height + BLOCK - 1) / BLOCK;
+    uint64_t ev = 0, co = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : ev, co)
+    for (int64_t tile = 0; tile < (int64_t)gx * gy; ++tile) {
+        const uint32_t tx = (uint32_t)(tile % gx), ty = (uint32_t)(tile / gx);
+        const uint32_t start = ranges[tile * 2], end = ranges[tile * 2 + 1];
+        for (uint32_t ly = 0; ly < BLOCK; ++ly)
+            for (uint32_t lx = 0; lx < BLOCK; ++lx) {
+                const uint32_t pxl = tx * BLOCK + lx, pyl = ty * BLOCK + ly;
+                if (pxl >= width || pyl >= height) continue;
+                const float fx = (float)pxl, fy = (float)pyl;
+                float T = 1.0f;
+                for (uint32_t k = start; k < end; ++k) {
+                    ++ev;
+                    const uint32_t* s = splats + (size_t)vals[k] * ORC_SPLAT_WORDS;
+                    const float dx = bitsf(s[4]) - fx, dy = bitsf(s[5]) - fy;
+                    const float cx = bitsf(s[8]), cy = bitsf(s[9]), cz = bitsf(s[10]);
+                    const float power = -0.5f * (cx * dx * dx + cz * dy * dy) - cy * dx * dy;
+                    if (power > 0.0f) continue;
+                    const float alpha = std::fmin(0.99f, bitsf(s[11]) * std::exp(power));
+                    if (alpha < 1.0f / 255.0f) continue;
+                    if (T * (1.0f - alpha) < 0.0001f) break;
+                    ++co;
+                    T = T * (1.0f - alpha);
+                }
+            }
+    }
+    *evaluated = ev;
+    *contributing = co;
+}
+
 // Decision windows for the FP64 blend's fragile flag.
 static constexpr double kPowWin = 1e-6, kAlphaRel = 1e-4, kTermRel = 1e-4;
 

@@ -95,6 +95,14 @@ void orc_blend_f32(const uint32_t* splats, const uint32_t* vals, const uint32_t*
                    uint32_t width, uint32_t height, float* image, float* final_T,
                    uint32_t* n_contrib, int threads);
 
+/* The work measure of the blend: (pixel, list entry) pairs evaluated until
+ * each pixel terminates, by the FP32 blend's rules (blend.slang:24-105: the
+ * entry that would bring T below 1e-4 is evaluated and ends the pixel), and
+ * the pairs that contribute colour. */
+void orc_blend_pair_count(const uint32_t* splats, const uint32_t* vals, const uint32_t* ranges,
+                          uint32_t width, uint32_t height, uint64_t* evaluated, uint64_t* contributing,
+                          int threads);
+
 /* Blend in FP64 over the same lists. splat64: n*12 doubles (orc_preprocess_f64).
  * fragile (may be NULL): 1 for pixels where an alpha / skip / termination
  * decision lies within a small window of its threshold. */

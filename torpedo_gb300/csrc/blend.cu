@@ -22,10 +22,11 @@
 // Warp culling: a warp owns an 8x4 pixel block of the tile. Each staged entry
 // carries the axis-aligned box of the ellipse on which alpha >= 1/255 can hold
 // (enlarged by a relative 2e-3 and 0.01 px); a warp ballots 32 entries at a
-// time against its block and walks only the entries whose box meets it. A
-// culled pair lies outside that ellipse, where the exact alpha is below 1/255
-// and the reference skips it too. Forward and adjoint use the same blocks and
-// boxes, so they cull the same pairs.
+// time against its block (box first, then the ellipse itself: the maximum of
+// p2 over the block) and walks only the entries that can reach it. A culled
+// pair lies outside that ellipse, where the exact alpha is below 1/255 and
+// the reference skips it too. Forward and adjoint use the same blocks and
+// tests, so they cull the same pairs.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 
@@ -98,6 +99,33 @@ __device__ __forceinline__ bool box_meets(float4 b, float x0, float y0) {
     return b.x <= x0 + 7.0f && b.y >= x0 && b.z <= y0 + 3.0f && b.w >= y0;
 }
 
+// Largest p2 on the rectangle's edge with d = (dx, fixed dy) or (fixed dx, dy).
+__device__ __forceinline__ float edge_p2(float4 q, float dx, float dy) {
+    const float f = q.x * dx * dx + q.y * dx * dy + q.z * dy * dy;
+    // a bound on the rounding of f in single precision, so the test stays conservative
+    const float mag = fabsf(q.x) * dx * dx + fabsf(q.y * dx * dy) + fabsf(q.z) * dy * dy;
+    return f + 1e-5f * mag;
+}
+
+// true when the entry can reach alpha >= 1/255 somewhere in the pixel block
+// [x0, x0+7] x [y0, y0+3]: p2 is a concave quadratic in (dx, dy), so its
+// maximum over the block is 0 at the centre when the centre lies inside,
+// else on an edge, at the edge's vertex clamped to the edge. The threshold is
+// lowered by 1e-3 |thr| + 1e-3 so rounding can only keep an entry, never cull
+// one the exact test keeps.
+__device__ __forceinline__ bool entry_meets_block(float2 c, float4 q, float4 b, float x0, float y0) {
+    if (!box_meets(b, x0, y0)) return false;
+    const float lox = x0 - c.x, hix = lox + 7.0f, loy = y0 - c.y, hiy = loy + 3.0f;
+    if (lox <= 0.0f && hix >= 0.0f && loy <= 0.0f && hiy >= 0.0f) return true;
+    const float ry = __fdividef(-0.5f * q.y, q.z);  // vertex of a vertical edge: dy = ry dx
+    const float rx = __fdividef(-0.5f * q.y, q.x);  // of a horizontal edge: dx = rx dy
+    float best = edge_p2(q, lox, fminf(fmaxf(ry * lox, loy), hiy));
+    best = fmaxf(best, edge_p2(q, hix, fminf(fmaxf(ry * hix, loy), hiy)));
+    best = fmaxf(best, edge_p2(q, fminf(fmaxf(rx * loy, lox), hix), loy));
+    best = fmaxf(best, edge_p2(q, fminf(fmaxf(rx * hiy, lox), hix), hiy));
+    return best >= q.w - (1e-3f * fabsf(q.w) + 1e-3f);
+}
+
 __device__ __forceinline__ float pair_p2(float2 xy, float4 q, float pxf, float pyf, float& dx, float& dy) {
     dx = __fsub_rn(xy.x, pxf);
     dy = __fsub_rn(xy.y, pyf);
@@ -168,28 +196,29 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
         for (uint32_t g = 0; g < n; g += 32) {
             if (__all_sync(0xFFFFFFFFu, done)) break;
             const uint32_t e = g + lane;
-            uint32_t m = __ballot_sync(0xFFFFFFFFu, e < n && box_meets(s_box[e], bxf, byf));
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, e < n && entry_meets_block(s_xy[e], s_q[e], s_box[e], bxf, byf));
+            // branch-free body: every lane evaluates the pair and selects the
+            // update, so a warp whose lanes take different decisions does not
+            // run the paths one after another
             while (m) {
                 const uint32_t jj = g + uint32_t(__ffs(m) - 1);
                 m &= m - 1u;
-                if (done) continue;
                 float dx, dy;
                 const float4 q = s_q[jj];
                 const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
-                if (pair_skipped(p2, q.w)) continue;
                 const float4 col = s_col[jj];
                 const float alpha = fminf(kAlphaMax, __fmul_rn(col.w, ex2_approx(p2)));
                 const float tn = __fmul_rn(T, __fsub_rn(1.0f, alpha));
-                if (tn < kTMin) {
-                    done = true;
-                    continue;
-                }
+                const bool live = !done && !pair_skipped(p2, q.w);
+                const bool term = live && tn < kTMin;
+                const bool add = live && !term;
+                done = done || term;
                 const float w = __fmul_rn(alpha, T);
-                C0 = __fmaf_rn(col.x, w, C0);
-                C1 = __fmaf_rn(col.y, w, C1);
-                C2 = __fmaf_rn(col.z, w, C2);
-                T = tn;
-                last = b0 + jj - start + 1;
+                C0 = add ? __fmaf_rn(col.x, w, C0) : C0;
+                C1 = add ? __fmaf_rn(col.y, w, C1) : C1;
+                C2 = add ? __fmaf_rn(col.z, w, C2) : C2;
+                T = add ? tn : T;
+                last = add ? b0 + jj - start + 1 : last;
             }
         }
     }
@@ -285,14 +314,15 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
         g1 = a.dL_dimage[p * 3 + 1];
         g2 = a.dL_dimage[p * 3 + 2];
     }
-    // the block walks back from the largest last-contributor index over its pixels
-    uint32_t max_last = last;
+    // the block walks back from the largest last-contributor index over its
+    // pixels; a warp takes entries below its own largest index only
+    uint32_t warp_last = last;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) max_last = max(max_last, __shfl_xor_sync(0xFFFFFFFFu, max_last, o));
+    for (int o = 16; o > 0; o >>= 1) warp_last = max(warp_last, __shfl_xor_sync(0xFFFFFFFFu, warp_last, o));
     __shared__ uint32_t s_max[kBlendThreads / 32];
-    if (lane == 0) s_max[tid >> 5] = max_last;
+    if (lane == 0) s_max[tid >> 5] = warp_last;
     __syncthreads();
-    max_last = 0;
+    uint32_t max_last = 0;
 #pragma unroll
     for (uint32_t w = 0; w < kBlendThreads / 32; ++w) max_last = max(max_last, s_max[w]);
 
@@ -313,52 +343,50 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
             }
             s_idx[tid] = idx;
         }
-        for (uint32_t k = tid; k < kBlendThreads * kG2DStride; k += kBlendThreads) (&s_acc[0][0])[k] = 0.f;
+        for (uint32_t k = tid; k < n * kG2DStride; k += kBlendThreads) (&s_acc[0][0])[k] = 0.f;
         __syncthreads();
-        for (uint32_t g = 0; g < n; g += 32) {
-            uint32_t m = __ballot_sync(0xFFFFFFFFu, g + lane < n && box_meets(s_box[g + lane], bxf, byf));
+        // entries jj >= skip have list positions r_end - 1 - jj below warp_last
+        const uint32_t skip = uint32_t(r_end) > warp_last ? uint32_t(r_end) - warp_last : 0u;
+        for (uint32_t g = skip & ~31u; g < n; g += 32) {
+            const uint32_t jl = g + lane;
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, jl < n && jl >= skip &&
+                                                        entry_meets_block(s_xy[jl], s_q[jl], s_box[jl], bxf, byf));
             while (m) {
                 const uint32_t jj = g + uint32_t(__ffs(m) - 1);
                 m &= m - 1u;
                 const uint32_t e = uint32_t(r_end) - 1u - jj;
+                // branch-free body (as in the forward): every lane evaluates,
+                // the selects keep only contributing pairs
+                float dx, dy;
+                const float4 q = s_q[jj];
+                const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
+                const float4 col = s_col[jj];
+                const bool contrib = inside && e < last && !pair_skipped(p2, q.w);
+                const float G = ex2_approx(p2);
+                const float raw = __fmul_rn(col.w, G);
+                const float alpha = fminf(kAlphaMax, raw);
+                const float inv = __frcp_rn(1.0f - alpha);
+                const float Tb = T * inv;  // transmittance in front of this entry
+                const float w = alpha * Tb;
+                const float dA = g0 * (col.x * Tb - S0 * inv) + g1 * (col.y * Tb - S1 * inv) +
+                                 g2 * (col.z * Tb - S2 * inv);
+                S0 = contrib ? fmaf(col.x, w, S0) : S0;
+                S1 = contrib ? fmaf(col.y, w, S1) : S1;
+                S2 = contrib ? fmaf(col.z, w, S2) : S2;
+                T = contrib ? Tb : T;
+                // power = p2 ln2; d power / d(dx, dy) = ln2 (2 qa dx + qb dy, 2 qc dy + qb dx)
+                const bool unclamped = contrib && raw <= kAlphaMax;
+                const float dpow = dA * alpha;
                 float gv[kG2D];
-#pragma unroll
-                for (int k = 0; k < kG2D; ++k) gv[k] = 0.f;
-                bool contrib = false;
-                if (inside && e < last) {
-                    float dx, dy;
-                    const float4 q = s_q[jj];
-                    const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
-                    if (!pair_skipped(p2, q.w)) {
-                        const float4 col = s_col[jj];
-                        const float G = ex2_approx(p2);
-                        const float raw = __fmul_rn(col.w, G);
-                        const float alpha = fminf(kAlphaMax, raw);
-                        contrib = true;
-                        const float inv = __frcp_rn(1.0f - alpha);
-                        const float Tb = T * inv;  // transmittance in front of this entry
-                        const float w = alpha * Tb;
-                        gv[6] = g0 * w;
-                        gv[7] = g1 * w;
-                        gv[8] = g2 * w;
-                        const float dA = g0 * (col.x * Tb - S0 * inv) + g1 * (col.y * Tb - S1 * inv) +
-                                         g2 * (col.z * Tb - S2 * inv);
-                        S0 = fmaf(col.x, w, S0);
-                        S1 = fmaf(col.y, w, S1);
-                        S2 = fmaf(col.z, w, S2);
-                        T = Tb;
-                        if (raw <= kAlphaMax) {
-                            // power = p2 ln2; d power / d(dx, dy) = ln2 (2 qa dx + qb dy, 2 qc dy + qb dx)
-                            const float dpow = dA * alpha;
-                            gv[5] = dA * G;
-                            gv[0] = dpow * kLn2 * (2.0f * q.x * dx + q.y * dy);
-                            gv[1] = dpow * kLn2 * (2.0f * q.z * dy + q.y * dx);
-                            gv[2] = dpow * (-0.5f * dx * dx);
-                            gv[3] = dpow * (-dx * dy);
-                            gv[4] = dpow * (-0.5f * dy * dy);
-                        }
-                    }
-                }
+                gv[0] = unclamped ? dpow * kLn2 * (2.0f * q.x * dx + q.y * dy) : 0.0f;
+                gv[1] = unclamped ? dpow * kLn2 * (2.0f * q.z * dy + q.y * dx) : 0.0f;
+                gv[2] = unclamped ? dpow * (-0.5f * dx * dx) : 0.0f;
+                gv[3] = unclamped ? dpow * (-dx * dy) : 0.0f;
+                gv[4] = unclamped ? dpow * (-0.5f * dy * dy) : 0.0f;
+                gv[5] = unclamped ? dA * G : 0.0f;
+                gv[6] = contrib ? g0 * w : 0.0f;
+                gv[7] = contrib ? g1 * w : 0.0f;
+                gv[8] = contrib ? g2 * w : 0.0f;
                 if (__any_sync(0xFFFFFFFFu, contrib)) {
                     const float lo[8] = {gv[0], gv[1], gv[2], gv[3], gv[4], gv[5], gv[6], gv[7]};
                     const float r = warp_sum8_transposed(lo, lane);
