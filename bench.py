@@ -320,6 +320,18 @@ def plain_views_rate(cfg_name, local, passes, settings):
     return passes * len(cams) / dt
 
 
+def run_train_only(args):
+    """cfg2 forward + backward steps alone (one JSON line), e.g. for a profiler."""
+    import torch
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream(torch.device("cuda", 0))
+    settings = {"sort_ctas_per_sm": args.sort_ctas or 3}
+    ms, st, _, _ = train_rate("cfg2", stream, 0, args.steps, args.warmup, settings)
+    print(json.dumps({"fwd_bwd": {"config": "cfg2", "value": round(1000.0 / ms, 3), "unit": "it/s",
+                                  "ms_per_step": round(ms, 4), "keys": int(st["keys"]), "settings": settings}}))
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -434,6 +446,24 @@ def run_ours(args):
     general = general_sort(eng, K, key_bits, stream, args.steps) if not args.no_general_sort else None
     eng.close()
 
+    # blend: evaluated (pixel, entry) pairs of this workload, counted on the CPU
+    # by the oracle's rules (oracle/count_blend_pairs.py) and committed
+    blend = None
+    pfile = ROOT / "profiles" / f"blend_pairs_{cfg.name}.json"
+    if pfile.exists():
+        pc = json.loads(pfile.read_text())
+        if int(pc["keys"]) == K:
+            sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+            fp32_peak = sm_count * 128 * 2 * float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+                                                   .get("sm_max_mhz", 2070.0)) * 1e6 / 1e12 \
+                if (ROOT / "MEASURED_PEAKS.json").exists() else sm_count * 128 * 2 * 2.07e9 / 1e12
+            pairs_s = pc["evaluated_pairs"] / (stage_avg["blend"] / 1000.0)
+            blend = {"kernel": "blend_kernel", "bound": "sm fp32 / issue", "evaluated_pairs": pc["evaluated_pairs"],
+                     "contributing_pairs": pc["contributing_pairs"], "ms": round(stage_avg["blend"], 4),
+                     "pairs_per_s": round(pairs_s, 1), "achieved_tflops": round(pairs_s * 20 / 1e12, 2),
+                     "peak_tflops": round(fp32_peak, 1), "frac": round(pairs_s * 20 / 1e12 / fp32_peak, 4),
+                     "note": "20 FP32 operations per evaluated pair; peak = SMs x 128 FP32 lanes x 2 x max SM clock"}
+
     fwd_bwd = batched = None
     if not args.no_train:
         ms2, st2, _, _ = train_rate("cfg2", stream, local, 50, 3, settings)
@@ -464,6 +494,7 @@ def run_ours(args):
                        "depth_sort_ms": round(stage_avg["depth_sort"], 4), "key_sort_ms": round(stage_avg["key_sort"], 4),
                        "note": "Gaussians sorted by depth first (N items), then the K keys on their tile-id bits only"},
         "general_sort": general,
+        "blend": blend,
         "stages_ms": {k: round(v, 4) for k, v in stage_avg.items()},
         "gpu_launches": launches_per_frame * args.steps,
         "clocks": clk,
@@ -499,9 +530,12 @@ def main():
     ap.add_argument("--sort-ctas", type=int, default=0,
                     help="radix pass kernel residency (2 or 3 CTAs per SM); 0 = autotune")
     ap.add_argument("--no-train", action="store_true", help="skip the cfg2 and cfg3 forward+backward measurements")
+    ap.add_argument("--train-only", action="store_true", help="only the cfg2 forward+backward steps (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.train_only:
+        run_train_only(args)
     else:
         run_ours(args)
 

@@ -66,7 +66,7 @@ typedef struct tpd_settings {
     double timeout_s;              /* host wait limit per frame in seconds (0: 60) */
     uint32_t test_never_publish;   /* test hook: scan partition 0 never publishes (exercises the bounded spin) */
     uint32_t stage_timing;         /* 1: frames run without a graph and record CUDA events between stages */
-    uint32_t sort_ctas_per_sm;     /* radix pass kernel residency: 2 (default, no register spills) or 3 */
+    uint32_t sort_ctas_per_sm;     /* radix pass kernel residency: 3 (0 = default) or 2 (no register spills) */
     uint32_t reserved[5];
 } tpd_settings;
 

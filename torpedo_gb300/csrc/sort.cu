@@ -293,7 +293,8 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
 }
 
 // CTAs per SM the onesweep kernel is compiled for: 2 (128 registers, no
-// spills) or 3 (80 registers). Chosen per engine (tpd_settings.sort_ctas_per_sm).
+// spills) or 3 (80 registers, the default: faster on the frame's passes).
+// Chosen per engine (tpd_settings.sort_ctas_per_sm).
 int g_onesweep_blocks_per_sm[4] = {0, 0, 0, 0};
 
 template <int kMinBlocks>
@@ -333,7 +334,7 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
     }
     if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
     const size_t smem = sizeof(OnesweepSmem);
-    const int variant = plan.ctas_per_sm == 3 ? 3 : 2;
+    const int variant = plan.ctas_per_sm == 2 ? 2 : 3;  // 0: the default, 3
     const int occ = variant == 3 ? onesweep_occupancy<3>(smem) : onesweep_occupancy<2>(smem);
     const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
     uint64_t* kin = keys;

@@ -149,7 +149,7 @@ class GaussianEngine:
 
     def __init__(self, sh_degree: int = 3, band3_compat: bool = True, device: int = 0, stream: int | None = None,
                  use_graph: bool = True, spin_limit: int = 0, initial_key_capacity: int = 0, timeout_s: float = 60.0,
-                 test_never_publish: bool = False, stage_timing: bool = False, sort_ctas_per_sm: int = 2):
+                 test_never_publish: bool = False, stage_timing: bool = False, sort_ctas_per_sm: int = 0):
         lib = L.load()
         s = L.Settings()
         lib.tpd_settings_init(C.byref(s))
