@@ -295,7 +295,7 @@ void enqueue_frame(tpd_engine* e) {
     pa.depth_items = e->d_ditems[0];
     pa.depth_key_bits = e->depth_key_bits;
     pa.ctl = e->d_ctl;
-    launch_preprocess(pa, s);
+    launch_preprocess(pa, e->num_sms, s);
     mark(1);
     const uint32_t spin = e->settings.spin_limit ? e->settings.spin_limit : kDefaultSpin;
     const uint32_t items = e->n * e->n_views;

@@ -53,7 +53,8 @@ __global__ void __launch_bounds__(kKeygenThreads)
 
     for (uint32_t wi = warp_global; wi < nwarps; wi += warps_total) {
         const uint32_t r = wi * 32u + lane;
-        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0, off = 0, depth_bits = 0, gi = 0, gx = 1, tile_base = 0;
+        // per item: its first tile (row-major in its view), rect width | view grid width << 16
+        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0, off = 0, depth_bits = 0, gi = 0, t0 = 0, wgx = 1u | (1u << 16);
         if (r < count) {
             const uint32_t item = items[r];
             off = offsets[r];
@@ -61,17 +62,17 @@ __global__ void __launch_bounds__(kKeygenThreads)
                 const uint32_t v = item / n;
                 gi = item - v * n;
                 const ViewConst& vc = views[v];
-                gx = grid_x(vc.width);
-                tile_base = vc.tile_base;
+                const uint32_t gx = grid_x(vc.width);
                 const float4 texel = reinterpret_cast<const float4*>(splats + item)[1];  // px, py, viewZ, radius
                 if (texel.w > 0.0f) {
                     bounding_rect(texel.x, texel.y, texel.w, gx, grid_y(vc.height), x0, y0, x1, y1);
                     depth_bits = __float_as_uint(texel.z);
                 }
+                t0 = vc.tile_base + y0 * gx + x0;
+                wgx = max(x1 - x0, 1u) | (gx << 16);
             }
         }
-        const uint32_t w = x1 - x0;
-        const uint32_t cnt = w * (y1 - y0);
+        const uint32_t cnt = (x1 - x0) * (y1 - y0);
         const uint32_t incl = warp_inclusive_scan(cnt);
         const uint32_t excl = incl - cnt;
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
@@ -86,23 +87,29 @@ __global__ void __launch_bounds__(kKeygenThreads)
                 const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, cand & 31u);
                 if (cand < 32u && e <= s) j = cand;
             }
-            const uint32_t jx0 = __shfl_sync(0xFFFFFFFFu, x0, j);
-            const uint32_t jy0 = __shfl_sync(0xFFFFFFFFu, y0, j);
-            const uint32_t jw = __shfl_sync(0xFFFFFFFFu, w, j);
+            const uint32_t jt0 = __shfl_sync(0xFFFFFFFFu, t0, j);
+            const uint32_t jwg = __shfl_sync(0xFFFFFFFFu, wgx, j);
             const uint32_t jex = __shfl_sync(0xFFFFFFFFu, excl, j);
             const uint32_t jdb = __shfl_sync(0xFFFFFFFFu, depth_bits, j);
             const uint32_t jgi = __shfl_sync(0xFFFFFFFFu, gi, j);
-            const uint32_t jgx = __shfl_sync(0xFFFFFFFFu, gx, j);
-            const uint32_t jtb = __shfl_sync(0xFFFFFFFFu, tile_base, j);
             uint32_t tile = 0;
             // a key past the capacity is dropped and not counted, so the sort
             // of an overflowed frame still sees a consistent histogram
             const bool live = s < total && uint64_t(base) + s < capacity;
             if (live) {
-                const uint32_t local = s - jex;
-                const uint32_t ty = jy0 + local / jw;
-                const uint32_t tx = jx0 + local % jw;
-                tile = jtb + ty * jgx + tx;
+                const uint32_t local = s - jex;  // < 2^24: exact in a float
+                const uint32_t jw = jwg & 0xFFFFu, jgx = jwg >> 16;
+                // row = local / jw from a float quotient, corrected by one step
+                uint32_t ty = __float2uint_rz(__fdividef(float(local), float(jw)));
+                int32_t rem = int32_t(local) - int32_t(ty * jw);
+                if (rem < 0) {
+                    --ty;
+                    rem += int32_t(jw);
+                } else if (rem >= int32_t(jw)) {
+                    ++ty;
+                    rem -= int32_t(jw);
+                }
+                tile = jt0 + ty * jgx + uint32_t(rem);
                 const uint64_t pos = uint64_t(base) + s;
                 keys[pos] = (uint64_t(tile) << 32) | uint64_t(jdb);
                 vals[pos] = jgi;

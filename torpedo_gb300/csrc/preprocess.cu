@@ -15,6 +15,8 @@
 // ticket). Arithmetic follows the shader source left to right with matrix
 // products accumulated k = 0..n-1; this file is compiled with --fmad=false so
 // no product is fused into an add.
+#include <algorithm>
+
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 #include "tpd_scan.cuh"
@@ -233,67 +235,88 @@ __device__ __forceinline__ uint32_t project_one(const Rec& rec, const float* em,
     return touched;
 }
 
+// Persistent CTAs over chunks of kPreThreads records: while a chunk is
+// projected, the next chunk's records stream into the other shared-memory
+// stage (one TMA bulk copy each), so HBM reads overlap the arithmetic.
+constexpr uint32_t kPreStages = 2;
+constexpr uint32_t kDepthPassesMax = 5;  // depth keys: 32 bits + log2(256 views)
+
+struct PreSmem {
+    float rec[kPreStages][kPreThreads * kRecordFloats];  // 30,720 B per stage, 16-byte multiple
+    uint32_t hist[kDepthPassesMax][256];                  // depth-key digit counts of this CTA
+    uint64_t bar[kPreStages];
+};
+
 __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs a) {
-    __shared__ __align__(128) float srec[kPreThreads * kRecordFloats];
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ uint32_t sh[8][256];  // depth-key digit counts of this CTA
+    extern __shared__ __align__(128) unsigned char pre_smem[];
+    PreSmem& S = *reinterpret_cast<PreSmem*>(pre_smem);
 
     const uint32_t tid = threadIdx.x;
-    for (uint32_t k = tid; k < 8 * 256; k += kPreThreads) (&sh[0][0])[k] = 0;
+    for (uint32_t k = tid; k < kDepthPassesMax * 256; k += kPreThreads) (&S.hist[0][0])[k] = 0;
     if (tid == 0) {
-        mbar_init(&bar, 1);
+        for (uint32_t st = 0; st < kPreStages; ++st) mbar_init(&S.bar[st], 1);
         fence_mbar_init();
     }
     __syncthreads();
-    const uint32_t base = blockIdx.x * kPreThreads;
-    const uint32_t cnt = min(kPreThreads, a.n - base);
-    if (tid == 0) {
-        const uint32_t bytes = cnt * kRecordBytes;  // multiple of 16 (240 = 15 x 16)
-        mbar_arrive_expect_tx(&bar, bytes);
-        bulk_copy_g2s(srec, a.recs + size_t(base) * kRecordFloats, bytes, &bar);
-    }
-    bool staged = mbar_wait_bounded(&bar, 0, &a.ctl->status);
-    if (!staged) mbar_wait_bounded(&bar, 0, &a.ctl->status, 1u << 26);  // never leave with the copy in flight
+    const uint32_t nchunks = (a.n + kPreThreads - 1) / kPreThreads;
+    const uint32_t npass = min(kDepthPassesMax, (a.depth_key_bits + 7) / 8);
+    auto issue = [&](uint32_t chunk, uint32_t stage) {
+        const uint32_t base = chunk * kPreThreads;
+        const uint32_t bytes = min(kPreThreads, a.n - base) * kRecordBytes;  // multiple of 16 (240 = 15 x 16)
+        mbar_arrive_expect_tx(&S.bar[stage], bytes);
+        bulk_copy_g2s(S.rec[stage], a.recs + size_t(base) * kRecordFloats, bytes, &S.bar[stage]);
+    };
+    if (tid == 0 && blockIdx.x < nchunks) issue(blockIdx.x, 0);
 
-    const uint32_t i = base + tid;
-    const uint32_t e = (tid < cnt && a.ent_idx) ? a.ent_idx[i] : 0u;
-    const uint32_t npass = (a.depth_key_bits + 7) / 8;
-    for (uint32_t v = 0; v < a.n_views; ++v) {
-        Splat sp;
-        uint32_t tiles = 0;
-        if (tid < cnt && staged) {
-            const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
-            float emr[kEntityMatFloats];
+    uint32_t it = 0;
+    for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, ++it) {
+        const uint32_t stage = it & 1u, parity = (it >> 1) & 1u;
+        // the other stage was released by the barrier that ended the last iteration
+        if (tid == 0 && chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, stage ^ 1u);
+        bool staged = mbar_wait_bounded(&S.bar[stage], parity, &a.ctl->status);
+        if (!staged) mbar_wait_bounded(&S.bar[stage], parity, &a.ctl->status, 1u << 26);  // never leave a copy in flight
+
+        const uint32_t base = chunk * kPreThreads;
+        const uint32_t cnt = min(kPreThreads, a.n - base);
+        const uint32_t i = base + tid;
+        const uint32_t e = (tid < cnt && a.ent_idx) ? a.ent_idx[i] : 0u;
+        for (uint32_t v = 0; v < a.n_views; ++v) {
+            Splat sp;
+            uint32_t tiles = 0;
+            if (tid < cnt && staged) {
+                const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
+                float emr[kEntityMatFloats];
 #pragma unroll
-            for (int k = 0; k < kEntityMatFloats; ++k) emr[k] = __ldg(em + k);
-            tiles = project_one(Rec{srec + tid * kRecordFloats}, emr, a.views[v], a.sh_degree, a.band3_compat != 0,
-                                sp);
-        } else {
-            sp = Splat{0.f, 0.f, 0.f, 0u, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        }
-        if (tid < cnt) {
-            const size_t item = size_t(v) * a.n + i;
-            float4* dst = reinterpret_cast<float4*>(a.splats + item);
-            const float4* src = reinterpret_cast<const float4*>(&sp);
-            dst[0] = src[0];
-            dst[1] = src[1];
-            dst[2] = src[2];
-            if (a.depth_keys) {
-                const uint64_t key = (uint64_t(v) << 32) | (tiles ? __float_as_uint(sp.depth) : 0xFFFFFFFFu);
-                a.depth_keys[item] = key;
-                a.depth_items[item] = uint32_t(item);
-                for (uint32_t p = 0; p < npass; ++p) {
-                    const uint32_t bits = min(8u, a.depth_key_bits - 8 * p);
-                    atomicAdd(&sh[p][uint32_t(key >> (8 * p)) & ((1u << bits) - 1u)], 1u);
+                for (int k = 0; k < kEntityMatFloats; ++k) emr[k] = __ldg(em + k);
+                tiles = project_one(Rec{S.rec[stage] + tid * kRecordFloats}, emr, a.views[v], a.sh_degree,
+                                    a.band3_compat != 0, sp);
+            } else {
+                sp = Splat{0.f, 0.f, 0.f, 0u, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            }
+            if (tid < cnt) {
+                const size_t item = size_t(v) * a.n + i;
+                float4* dst = reinterpret_cast<float4*>(a.splats + item);
+                const float4* src = reinterpret_cast<const float4*>(&sp);
+                dst[0] = src[0];
+                dst[1] = src[1];
+                dst[2] = src[2];
+                if (a.depth_keys) {
+                    const uint64_t key = (uint64_t(v) << 32) | (tiles ? __float_as_uint(sp.depth) : 0xFFFFFFFFu);
+                    a.depth_keys[item] = key;
+                    a.depth_items[item] = uint32_t(item);
+                    for (uint32_t p = 0; p < npass; ++p) {
+                        const uint32_t bits = min(8u, a.depth_key_bits - 8 * p);
+                        atomicAdd(&S.hist[p][uint32_t(key >> (8 * p)) & ((1u << bits) - 1u)], 1u);
+                    }
                 }
             }
         }
+        __syncthreads();  // every thread is done with this stage before it is refilled
     }
     if (!a.depth_keys) return;
-    __syncthreads();
     for (uint32_t p = 0; p < npass; ++p)
         for (uint32_t d = tid; d < 256; d += kPreThreads)
-            if (sh[p][d]) atomicAdd(&a.ctl->depth_hist[p][d], sh[p][d]);
+            if (S.hist[p][d]) atomicAdd(&a.ctl->depth_hist[p][d], S.hist[p][d]);
 }
 
 // Exclusive scan of tile counts over partitions of 256 threads x 4 items
@@ -377,10 +400,18 @@ void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, 
     frame_begin_kernel<<<1, 256, 0, s>>>(ctl, transforms, n_ent, views, n_views, ent_mats);
 }
 
-void launch_preprocess(const PreprocessArgs& a, cudaStream_t s) {
+void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s) {
     if (a.n == 0 || a.n_views == 0) return;
-    const uint32_t blocks = (a.n + kPreThreads - 1) / kPreThreads;
-    preprocess_kernel<<<blocks, kPreThreads, 0, s>>>(a);
+    static int per_sm = 0;  // resident CTAs per SM at this shared-memory size (same on every GB300)
+    if (per_sm == 0) {
+        cudaFuncSetAttribute(preprocess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(PreSmem)));
+        int r = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, preprocess_kernel, kPreThreads, sizeof(PreSmem));
+        per_sm = r > 0 ? r : 1;
+    }
+    const uint32_t chunks = (a.n + kPreThreads - 1) / kPreThreads;
+    const uint32_t blocks = std::min<uint32_t>(chunks, uint32_t((num_sms > 0 ? num_sms : 148) * per_sm));
+    preprocess_kernel<<<blocks, kPreThreads, sizeof(PreSmem), s>>>(a);
 }
 
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,

@@ -61,7 +61,7 @@ constexpr uint32_t kMaxViews = 256;
 // entity matrices for n_views x n_ent (transforms nullptr -> identity).
 void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, const ViewConst* views,
                         uint32_t n_views, float* ent_mats, cudaStream_t s);
-void launch_preprocess(const PreprocessArgs& a, cudaStream_t s);
+void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s);
 
 // Tile counts of (view, Gaussian) items in depth order, gathered through
 // items[r] = v * n + i, scanned into exclusive key offsets offsets[r]; the total
