@@ -30,7 +30,8 @@ class Settings(C.Structure):
         ("test_never_publish", C.c_uint32),
         ("stage_timing", C.c_uint32),
         ("sort_ctas_per_sm", C.c_uint32),
-        ("reserved", C.c_uint32 * 5),
+        ("depth_sort_items", C.c_uint32),
+        ("reserved", C.c_uint32 * 4),
     ]
 
 

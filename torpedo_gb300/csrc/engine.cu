@@ -177,7 +177,7 @@ int ensure_splat_buffers(tpd_engine* e) {
             TPD_CUDA(e, dalloc(e->d_dkeys[b], need));
             TPD_CUDA(e, dalloc(e->d_ditems[b], need));
         }
-        const size_t de = sort_desc_entries(uint32_t(need));
+        const size_t de = sort_desc_entries(uint32_t(need), 4);  // room for the smallest partitions
         TPD_CUDA(e, dalloc(e->d_desc_depth, de));
         TPD_CUDA(e, cudaMemset(e->d_desc_depth, 0, de * 8));
         e->splat_cap = need;
@@ -307,6 +307,7 @@ void enqueue_frame(tpd_engine* e) {
     dp.ticket_base = kTicketDepthSortBase;
     dp.tag_base = kTagDepthSort;
     dp.ctas_per_sm = int(e->settings.sort_ctas_per_sm);
+    dp.items = e->settings.depth_sort_items == 4 || e->settings.depth_sort_items == 16 ? e->settings.depth_sort_items : 8;
     dp.fixed_count = items;
     e->depth_in_alt = launch_sort(e->d_dkeys[0], e->d_ditems[0], e->d_dkeys[1], e->d_ditems[1], items, dp,
                                   e->d_desc_depth, e->d_ctl, spin, e->num_sms, s);

@@ -35,8 +35,11 @@ constexpr uint32_t kRadixBits = 8;
 constexpr uint32_t kRadix = 1u << kRadixBits;
 constexpr uint32_t kSortThreads = 256;
 constexpr uint32_t kSortWarps = kSortThreads / 32;
-constexpr uint32_t kSortItems = 16;
-constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // 4096 keys per partition
+// Keys per thread of a radix pass: 16 (4096-key partitions) for large sorts;
+// 8 or 4 give more, shorter partitions when the sort is too small to fill the
+// GPU with 4096-key partitions (the depth sort of 1M Gaussians).
+constexpr uint32_t kSortItemsMax = 16;
+constexpr uint32_t kSortTileMax = kSortThreads * kSortItemsMax;
 constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K
 
 constexpr uint32_t kHistThreads = 256;
@@ -46,12 +49,13 @@ constexpr uint32_t kHistChunk = 2048;  // keys per TMA chunk (16 KB)
 // (8-bit digits over a 4096-key partition) put the runs of consecutive digits
 // 128 B apart, which without padding lands a warp's stores on one bank when
 // its lanes carry consecutive digits (keys of one Gaussian's tile rectangle).
-constexpr uint32_t kSortTilePadded = kSortTile + kSortTile / 16;
 __device__ __forceinline__ uint32_t pad16(uint32_t i) { return i + (i >> 4); }
 
+template <int kItems>
 struct OnesweepSmem {
-    uint64_t keys[kSortTilePadded];
-    uint32_t vals[kSortTilePadded];
+    static constexpr uint32_t kTile = kSortThreads * kItems;
+    uint64_t keys[kTile + kTile / 16];
+    uint32_t vals[kTile + kTile / 16];
     uint32_t whist[kSortWarps][kRadix];
     uint32_t gdig[kRadix];    // global exclusive digit offsets of this pass
     uint32_t lstart[kRadix];  // block-local digit start
@@ -172,7 +176,7 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
     return excl;
 }
 
-template <int kMinBlocks>
+template <int kItems, int kMinBlocks>
 __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
     onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
@@ -180,7 +184,8 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
                     uint32_t tag_slot, uint32_t fixed_count, uint64_t* __restrict__ desc, FrameCtl* ctl,
                     uint32_t spin_limit) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    OnesweepSmem& S = *reinterpret_cast<OnesweepSmem*>(smem_raw);
+    constexpr uint32_t kSortItems = kItems, kSortTile = kSortThreads * kItems;
+    OnesweepSmem<kItems>& S = *reinterpret_cast<OnesweepSmem<kItems>*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
     const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
@@ -292,29 +297,51 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
     }
 }
 
-// CTAs per SM the onesweep kernel is compiled for: 2 (128 registers, no
+// CTAs per SM the 16-key variant is compiled for: 2 (128 registers, no
 // spills) or 3 (80 registers, the default: faster on the frame's passes).
-// Chosen per engine (tpd_settings.sort_ctas_per_sm).
-int g_onesweep_blocks_per_sm[4] = {0, 0, 0, 0};
-
-template <int kMinBlocks>
-int onesweep_occupancy(size_t smem) {
-    int& b = g_onesweep_blocks_per_sm[kMinBlocks];
+// Chosen per engine (tpd_settings.sort_ctas_per_sm). The 8- and 4-key
+// variants are compiled for 4 and 5 CTAs per SM.
+template <int kItems, int kMinBlocks>
+int onesweep_occupancy() {
+    static int b = 0;
     if (b == 0) {
-        cudaFuncSetAttribute(onesweep_kernel<kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        const size_t smem = sizeof(OnesweepSmem<kItems>);
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem));
         int r = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kMinBlocks>, kSortThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kMinBlocks>, kSortThreads, smem);
         b = r > 0 ? r : 1;
     }
     return b;
+}
+
+template <int kItems, int kMinBlocks>
+void launch_passes(uint64_t* kin, uint32_t* vin, uint64_t* kout, uint32_t* vout, uint32_t capacity, uint32_t p0,
+                   uint32_t p1, const SortPlan& plan, uint32_t (*hist)[256], uint64_t* desc, FrameCtl* ctl,
+                   uint32_t spin_limit, int sms, cudaStream_t s) {
+    const size_t smem = sizeof(OnesweepSmem<kItems>);
+    const int occ = onesweep_occupancy<kItems, kMinBlocks>();
+    const uint32_t tile = kSortThreads * kItems;
+    const uint32_t max_parts = (capacity + tile - 1) / tile;
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
+    for (uint32_t p = p0; p < p1; ++p) {
+        const uint32_t shift = p * kRadixBits;
+        const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
+        onesweep_kernel<kItems, kMinBlocks><<<grid, kSortThreads, smem, s>>>(
+            kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p, plan.tag_base + p,
+            plan.fixed_count, desc, ctl, spin_limit);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
 }
 
 }  // namespace
 
 uint32_t sort_pass_count(uint32_t key_bits) { return (key_bits + kRadixBits - 1) / kRadixBits; }
 
-size_t sort_desc_entries(uint32_t capacity) {
-    return (size_t(capacity) + kSortTile - 1) / kSortTile * kRadix + kRadix;
+size_t sort_desc_entries(uint32_t capacity, uint32_t items) {
+    const size_t tile = size_t(kSortThreads) * (items ? items : kSortItemsMax);
+    return (size_t(capacity) + tile - 1) / tile * kRadix + kRadix;
 }
 
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s) { sort_begin_kernel<<<1, 256, 0, s>>>(ctl, total); }
@@ -326,34 +353,22 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
     const uint32_t p1 = std::min(8u, sort_pass_count(plan.key_bits));
     if (p1 <= p0 || capacity == 0) return false;
     const int sms = num_sms > 0 ? num_sms : 148;
-    const uint32_t max_parts = (capacity + kSortTile - 1) / kSortTile;
     uint32_t (*hist)[256] = plan.hist ? plan.hist : ctl->sort_hist;
     if (!plan.hist_ready) {
         const uint32_t hist_blocks = std::max(1u, std::min<uint32_t>(uint32_t(sms) * 4u, capacity / kHistChunk + 1u));
         sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, p0, p1, plan.key_bits, hist, ctl);
     }
     if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
-    const size_t smem = sizeof(OnesweepSmem);
-    const int variant = plan.ctas_per_sm == 2 ? 2 : 3;  // 0: the default, 3
-    const int occ = variant == 3 ? onesweep_occupancy<3>(smem) : onesweep_occupancy<2>(smem);
-    const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
-    uint64_t* kin = keys;
-    uint32_t* vin = vals;
-    uint64_t* kout = keys_alt;
-    uint32_t* vout = vals_alt;
-    for (uint32_t p = p0; p < p1; ++p) {
-        const uint32_t shift = p * kRadixBits;
-        const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
-        const uint32_t ticket = plan.ticket_base + p, tag = plan.tag_base + p;
-        if (variant == 3)
-            onesweep_kernel<3><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist,
-                                                                ticket, tag, plan.fixed_count, desc, ctl, spin_limit);
-        else
-            onesweep_kernel<2><<<grid, kSortThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist,
-                                                                ticket, tag, plan.fixed_count, desc, ctl, spin_limit);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
+    if (plan.items == 8)
+        launch_passes<8, 4>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms, s);
+    else if (plan.items == 4)
+        launch_passes<4, 5>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms, s);
+    else if (plan.ctas_per_sm == 2)
+        launch_passes<16, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms,
+                             s);
+    else
+        launch_passes<16, 3>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms,
+                             s);
     return ((p1 - p0) & 1u) != 0;
 }
 

@@ -87,8 +87,8 @@ void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* o
 // histogram kernel builds them); tickets ctl->ticket[ticket_base + position];
 // look-back tags ctl->tag * 32 + tag_base + position. Result in (keys, vals)
 // for an even pass count, else in (keys_alt, vals_alt); returns true for *_alt.
-// desc: sort_desc_entries(capacity) descriptors (tagged, never cleared).
-size_t sort_desc_entries(uint32_t capacity);
+// desc: sort_desc_entries(capacity, items) descriptors (tagged, never cleared).
+size_t sort_desc_entries(uint32_t capacity, uint32_t items = 16);
 uint32_t sort_pass_count(uint32_t key_bits);
 struct SortPlan {
     uint32_t first_bit = 0;
@@ -98,6 +98,7 @@ struct SortPlan {
     uint32_t ticket_base = kTicketKeySortBase;
     uint32_t tag_base = kTagKeySort;
     int ctas_per_sm = 2;
+    uint32_t items = 16;               // keys per thread: 16 (4096-key partitions), 8 or 4
     uint32_t fixed_count = 0;          // nonzero: sort this many pairs, else min(ctl->total_keys, capacity)
     cudaEvent_t after_hist = nullptr;  // recorded between the histogram and the first pass
 };
