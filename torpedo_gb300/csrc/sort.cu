@@ -214,10 +214,15 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         // packs the digit (bits 0..8, kInvalidDigit past K) and the key's rank
         // among equal digits earlier in the warp (bits 9..31).
         uint64_t k[kSortItems];
+        // variants with registers to spare load the values with the keys, so
+        // the two loads share one memory latency
+        constexpr bool kValsEarly = kItems * kMinBlocks <= 32;
+        uint32_t vr[kValsEarly ? kSortItems : 1];
 #pragma unroll
         for (uint32_t i = 0; i < kSortItems; ++i) {
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
             k[i] = idx < cnt ? keys_in[base + idx] : ~0ull;
+            if constexpr (kValsEarly) vr[i] = idx < cnt ? vals_in[base + idx] : 0u;
         }
         uint32_t dr[kSortItems];
         const uint32_t lt = lanemask_lt();
@@ -267,7 +272,9 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
             const uint32_t d = dr[i] & 511u;
             if (d < kRadix) {
-                const uint32_t v = vals_in[base + idx];
+                uint32_t v;
+                if constexpr (kValsEarly) v = vr[i];
+                else v = vals_in[base + idx];
                 const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
                 if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pad16(pos)] = v;
             }
