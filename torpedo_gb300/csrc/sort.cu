@@ -230,7 +230,22 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         for (uint32_t i = 0; i < kSortItems; ++i) {
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
             const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
-            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+            // lanes with the same digit: one ballot per digit bit (the pass's
+            // `bits`, plus bit 8 for the past-the-end digit)
+            uint32_t peers = 0xFFFFFFFFu;
+#pragma unroll
+            for (uint32_t b = 0; b < kRadixBits; ++b) {
+                if (b < bits) {
+                    const bool on = (d >> b) & 1u;
+                    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+                    peers &= on ? bal : ~bal;
+                }
+            }
+            {
+                const bool on = d >= kRadix;
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+                peers &= on ? bal : ~bal;
+            }
             const uint32_t leader = __ffs(peers) - 1;
             uint32_t prev = 0;
             if (lane == leader && d < kRadix) {
