@@ -68,7 +68,8 @@ typedef struct tpd_settings {
     uint32_t stage_timing;         /* 1: frames run without a graph and record CUDA events between stages */
     uint32_t sort_ctas_per_sm;     /* radix pass kernel residency: 3 (0 = default) or 2 (no register spills) */
     uint32_t depth_sort_items;     /* keys per thread of the depth sort's radix passes: 4, 8 or 16 (0 = default 8) */
-    uint32_t reserved[4];
+    uint32_t sort_threads;         /* radix pass CTA size for 4096-key partitions: 256 (0 = default) or 512 (8 keys each) */
+    uint32_t reserved[3];
 } tpd_settings;
 
 /* Stages of a frame, for tpd_stage_times. */

@@ -31,7 +31,8 @@ class Settings(C.Structure):
         ("stage_timing", C.c_uint32),
         ("sort_ctas_per_sm", C.c_uint32),
         ("depth_sort_items", C.c_uint32),
-        ("reserved", C.c_uint32 * 4),
+        ("sort_threads", C.c_uint32),
+        ("reserved", C.c_uint32 * 3),
     ]
 
 

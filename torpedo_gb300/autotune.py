@@ -6,8 +6,10 @@ fastest, one axis at a time (each axis tried with the best values found so
 far for the others). The tunables are engine settings that leave every
 result bit for bit unchanged:
 
-  sort_ctas_per_sm   residency the 4096-key radix pass kernel is compiled for
-                     (2: 128 registers, no spills; 3: 80 registers)
+  sort_threads       CTA size of the 4096-key radix passes: 256 threads x 16
+                     keys, or 512 threads x 8 keys (twice the warps per SM)
+  sort_ctas_per_sm   residency the 256-thread radix pass kernel is compiled
+                     for (2: 128 registers, no spills; 3: 80 registers)
   depth_sort_items   keys per thread of the depth sort's radix passes (4, 8,
                      16: partitions of 1024, 2048, 4096 keys); smaller
                      partitions fill the GPU when the Gaussians are few
@@ -20,7 +22,7 @@ from __future__ import annotations
 
 from typing import Callable
 
-AXES = (("sort_ctas_per_sm", (3, 2)), ("depth_sort_items", (8, 4, 16)))
+AXES = (("sort_threads", (256, 512)), ("sort_ctas_per_sm", (2, 3)), ("depth_sort_items", (16, 8)))
 
 
 def time_steps(make_engine: Callable[[dict], object], enqueue: Callable[[object, int], None], stream,

@@ -51,16 +51,16 @@ constexpr uint32_t kHistChunk = 2048;  // keys per TMA chunk (16 KB)
 // its lanes carry consecutive digits (keys of one Gaussian's tile rectangle).
 __device__ __forceinline__ uint32_t pad16(uint32_t i) { return i + (i >> 4); }
 
-template <int kItems>
+template <int kItems, int kThreads>
 struct OnesweepSmem {
-    static constexpr uint32_t kTile = kSortThreads * kItems;
+    static constexpr uint32_t kTile = kThreads * kItems;
     uint64_t keys[kTile + kTile / 16];
     uint32_t vals[kTile + kTile / 16];
-    uint32_t whist[kSortWarps][kRadix];
+    uint32_t whist[kThreads / 32][kRadix];
     uint32_t gdig[kRadix];    // global exclusive digit offsets of this pass
     uint32_t lstart[kRadix];  // block-local digit start
     uint32_t gmap[kRadix];    // global position of local index 0 of each digit
-    uint32_t wsum[kSortWarps];
+    uint32_t wsum[kThreads / 32];
     uint32_t part;
 };
 
@@ -70,7 +70,8 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-// Block-wide exclusive scan of one value per thread (256 threads); returns the exclusive prefix.
+// Block-wide exclusive scan of one value per thread (kWarps warps); returns the exclusive prefix.
+template <uint32_t kWarps = kSortWarps>
 __device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t* wsum) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t incl = warp_inclusive_scan(v);
@@ -78,7 +79,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t
     __syncthreads();
     uint32_t base = 0;
 #pragma unroll
-    for (uint32_t w = 0; w < kSortWarps; ++w)
+    for (uint32_t w = 0; w < kWarps; ++w)
         if (w < warp) base += wsum[w];
     __syncthreads();
     return base + incl - v;
@@ -176,16 +177,19 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
     return excl;
 }
 
-template <int kItems, int kMinBlocks>
-__global__ void __launch_bounds__(kSortThreads, kMinBlocks)
+// kThreads = 256 (one digit per thread) or 512 (the digit-wide steps run on
+// the first 256 threads); a partition is kThreads * kItems keys.
+template <int kItems, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
                     uint32_t pass, uint32_t shift, uint32_t bits, const uint32_t (*hist)[256], uint32_t ticket_slot,
                     uint32_t tag_slot, uint32_t fixed_count, uint64_t* __restrict__ desc, FrameCtl* ctl,
                     uint32_t spin_limit) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    constexpr uint32_t kSortItems = kItems, kSortTile = kSortThreads * kItems;
-    OnesweepSmem<kItems>& S = *reinterpret_cast<OnesweepSmem<kItems>*>(smem_raw);
+    constexpr uint32_t kSortItems = kItems, kSortTile = kThreads * kItems, kWarps = kThreads / 32;
+    OnesweepSmem<kItems, kThreads>& S = *reinterpret_cast<OnesweepSmem<kItems, kThreads>*>(smem_raw);
+    const bool digit_thread = threadIdx.x < kRadix;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
     const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
@@ -194,15 +198,15 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
 
     // global exclusive digit offsets (histogram of this pass, scanned)
     {
-        const uint32_t h = TPD_INBOUNDS(ctl, 16, pass, 8) ? hist[pass][tid] : 0u;
-        const uint32_t ex = block_exclusive_scan256(h, S.wsum);
-        S.gdig[tid] = ex;
+        const uint32_t h = digit_thread && TPD_INBOUNDS(ctl, 16, pass, 8) ? hist[pass][tid] : 0u;
+        const uint32_t ex = block_exclusive_scan256<kWarps>(h, S.wsum);
+        if (digit_thread) S.gdig[tid] = ex;
     }
 
     while (true) {
         if (tid == 0) S.part = atomicAdd(&ctl->ticket[ticket_slot], 1u);
 #pragma unroll
-        for (uint32_t w = 0; w < kSortWarps; ++w) S.whist[w][tid] = 0;
+        for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
         __syncthreads();
         const uint32_t part = S.part;
         if (part >= nparts) break;
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         uint64_t k[kSortItems];
         // variants with registers to spare load the values with the keys, so
         // the two loads share one memory latency
-        constexpr bool kValsEarly = kItems * kMinBlocks <= 32;
+        constexpr bool kValsEarly = kItems * kMinBlocks * (kThreads / 256) <= 32;
         uint32_t vr[kValsEarly ? kSortItems : 1];
 #pragma unroll
         for (uint32_t i = 0; i < kSortItems; ++i) {
@@ -260,16 +264,19 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
 
         // per digit (thread = digit): warp prefixes, block count, local start
         uint32_t count = 0;
+        uint64_t* dp = nullptr;
+        if (digit_thread) {
 #pragma unroll
-        for (uint32_t w = 0; w < kSortWarps; ++w) {
-            const uint32_t c = S.whist[w][tid];
-            S.whist[w][tid] = count;
-            count += c;
+            for (uint32_t w = 0; w < kWarps; ++w) {
+                const uint32_t c = S.whist[w][tid];
+                S.whist[w][tid] = count;
+                count += c;
+            }
+            dp = desc + size_t(TPD_INBOUNDS(ctl, 13, part, nparts) ? part : 0) * kRadix + tid;
+            st_relaxed_u64(dp, make_desc(part == 0 ? kFlagPrefix : kFlagAggregate, tag, count));
         }
-        uint64_t* dp = desc + size_t(TPD_INBOUNDS(ctl, 13, part, nparts) ? part : 0) * kRadix + tid;
-        st_relaxed_u64(dp, make_desc(part == 0 ? kFlagPrefix : kFlagAggregate, tag, count));
-        const uint32_t lstart = block_exclusive_scan256(count, S.wsum);  // (its barriers cover whist)
-        S.lstart[tid] = lstart;
+        const uint32_t lstart = block_exclusive_scan256<kWarps>(count, S.wsum);  // (its barriers cover whist)
+        if (digit_thread) S.lstart[tid] = lstart;
         __syncthreads();
 
         // reorder the partition in shared memory (stable: warp, then item, then
@@ -296,17 +303,19 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
         }
 
         // decoupled look-back for this thread's digit
-        if (part > 0) {
-            const uint32_t excl = digit_lookback(desc, part, tid, tag, ctl, spin_limit);
-            st_relaxed_u64(dp, make_desc(kFlagPrefix, tag, excl + count));
-            S.gmap[tid] = S.gdig[tid] + excl - lstart;
-        } else {
-            S.gmap[tid] = S.gdig[tid] - lstart;
+        if (digit_thread) {
+            if (part > 0) {
+                const uint32_t excl = digit_lookback(desc, part, tid, tag, ctl, spin_limit);
+                st_relaxed_u64(dp, make_desc(kFlagPrefix, tag, excl + count));
+                S.gmap[tid] = S.gdig[tid] + excl - lstart;
+            } else {
+                S.gmap[tid] = S.gdig[tid] - lstart;
+            }
         }
         __syncthreads();
 
         // coalesced write-out of digit runs
-        for (uint32_t j = tid; j < cnt; j += kSortThreads) {
+        for (uint32_t j = tid; j < cnt; j += kThreads) {
             const uint64_t key = S.keys[pad16(j)];
             const uint32_t d = uint32_t(key >> shift) & mask;
             const uint32_t g = S.gmap[d] + j;
@@ -319,37 +328,38 @@ __global__ void __launch_bounds__(kSortThreads, kMinBlocks)
     }
 }
 
-// CTAs per SM the 16-key variant is compiled for: 2 (128 registers, no
-// spills) or 3 (80 registers, the default: faster on the frame's passes).
-// Chosen per engine (tpd_settings.sort_ctas_per_sm). The 8- and 4-key
-// variants are compiled for 4 and 5 CTAs per SM.
-template <int kItems, int kMinBlocks>
+// Residencies: the 256-thread, 16-key variant is compiled for 2 CTAs per SM
+// (128 registers, no spills; the default) or 3 (80 registers); the 512-thread,
+// 8-key variant for 2 (32 warps per SM); the 8- and 4-key 256-thread variants
+// (shorter partitions, for small sorts) for 4 and 5.
+template <int kItems, int kThreads, int kMinBlocks>
 int onesweep_occupancy() {
     static int b = 0;
     if (b == 0) {
-        const size_t smem = sizeof(OnesweepSmem<kItems>);
-        cudaFuncSetAttribute(onesweep_kernel<kItems, kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(smem));
+        const size_t smem = sizeof(OnesweepSmem<kItems, kThreads>);
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         int r = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kMinBlocks>, kSortThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kThreads, kMinBlocks>, kThreads,
+                                                      smem);
         b = r > 0 ? r : 1;
     }
     return b;
 }
 
-template <int kItems, int kMinBlocks>
+template <int kItems, int kThreads, int kMinBlocks>
 void launch_passes(uint64_t* kin, uint32_t* vin, uint64_t* kout, uint32_t* vout, uint32_t capacity, uint32_t p0,
                    uint32_t p1, const SortPlan& plan, uint32_t (*hist)[256], uint64_t* desc, FrameCtl* ctl,
                    uint32_t spin_limit, int sms, cudaStream_t s) {
-    const size_t smem = sizeof(OnesweepSmem<kItems>);
-    const int occ = onesweep_occupancy<kItems, kMinBlocks>();
-    const uint32_t tile = kSortThreads * kItems;
+    const size_t smem = sizeof(OnesweepSmem<kItems, kThreads>);
+    const int occ = onesweep_occupancy<kItems, kThreads, kMinBlocks>();
+    const uint32_t tile = kThreads * kItems;
     const uint32_t max_parts = (capacity + tile - 1) / tile;
     const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
     for (uint32_t p = p0; p < p1; ++p) {
         const uint32_t shift = p * kRadixBits;
         const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
-        onesweep_kernel<kItems, kMinBlocks><<<grid, kSortThreads, smem, s>>>(
+        onesweep_kernel<kItems, kThreads, kMinBlocks><<<grid, kThreads, smem, s>>>(
             kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p, plan.tag_base + p,
             plan.fixed_count, desc, ctl, spin_limit);
         std::swap(kin, kout);
@@ -382,15 +392,20 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
     }
     if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
     if (plan.items == 8)
-        launch_passes<8, 4>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms, s);
+        launch_passes<8, 256, 4>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
+                                 sms, s);
     else if (plan.items == 4)
-        launch_passes<4, 5>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms, s);
-    else if (plan.ctas_per_sm == 2)
-        launch_passes<16, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms,
-                             s);
+        launch_passes<4, 256, 5>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
+                                 sms, s);
+    else if (plan.threads == 512)
+        launch_passes<8, 512, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
+                                 sms, s);
+    else if (plan.ctas_per_sm == 3)
+        launch_passes<16, 256, 3>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
+                                  sms, s);
     else
-        launch_passes<16, 3>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit, sms,
-                             s);
+        launch_passes<16, 256, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
+                                  sms, s);
     return ((p1 - p0) & 1u) != 0;
 }
 
