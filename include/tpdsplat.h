@@ -78,7 +78,7 @@ enum {
     TPD_STAGE_DEPTH_SORT = 1, /* radix sort of the (view | depth) keys, tile-count scan in depth order */
     TPD_STAGE_KEYGEN = 2,     /* key duplication in depth order */
     TPD_STAGE_KEY_SORT = 3,   /* radix sort of the (tile | depth) keys on their tile-id bits */
-    TPD_STAGE_RANGES = 4,     /* tile ranges (clear + kernel) */
+    TPD_STAGE_RANGES = 4,     /* empty: the key sort's last pass writes the tile ranges */
     TPD_STAGE_BLEND = 5,      /* alpha blend */
     TPD_STAGE_COUNT = 6
 };

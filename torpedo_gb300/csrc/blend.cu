@@ -174,7 +174,11 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     const bool inside = pxl < W && pyl < H;
     const float pxf = float(pxl), pyf = float(pyl);
     const uint32_t K = min(a.ctl->total_keys, a.capacity);
-    const uint32_t end = min(a.ranges[tile * 2 + 1], K), start = min(a.ranges[tile * 2 + 0], end);
+    const uint32_t raw_start = a.ranges[tile * 2 + 0], raw_end = a.ranges[tile * 2 + 1];
+    const uint32_t end = min(raw_end, K), start = min(raw_start, end);
+    // a tile without keys still holds the sort's preset (0xFFFFFFFF, 0): store
+    // the reference's empty range (0, 0)
+    if (tid == 0 && raw_start > raw_end) a.ranges[tile * 2 + 0] = 0u;
     const Splat* vsplats = a.splats + size_t(vi) * a.n;
 
     bool done = !inside;

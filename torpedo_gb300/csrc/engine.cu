@@ -318,7 +318,7 @@ void enqueue_frame(tpd_engine* e) {
     mark(2);
     const uint32_t cap = uint32_t(e->capacity);
     launch_keygen(e->d_splats, order, e->d_offsets, items, e->n, e->d_views, e->d_keys[0], e->d_vals[0], cap,
-                  e->key_bits, e->d_ctl, e->num_sms, s);
+                  e->key_bits, e->d_ranges, e->total_tiles, e->d_ctl, e->num_sms, s);
     mark(3);
     SortPlan kp;
     kp.first_bit = 32;  // the low 32 bits (depth) are already in order
@@ -329,12 +329,13 @@ void enqueue_frame(tpd_engine* e) {
     kp.tag_base = kTagKeySort;
     kp.ctas_per_sm = int(e->settings.sort_ctas_per_sm);
     kp.threads = e->settings.sort_threads == 512 ? 512 : 256;
+    kp.ranges = e->d_ranges;  // the last pass writes the tile ranges
+    kp.n_tiles = e->total_tiles;
     e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, kp, e->d_desc_sort,
                                    e->d_ctl, spin, e->num_sms, s);
     mark(4);
     const int b = e->sorted_in_alt ? 1 : 0;
-    launch_tile_ranges(e->d_keys[b], e->total_tiles, e->d_ranges, e->d_ctl, cap, e->num_sms, s);
-    mark(5);
+    mark(5);  // (tile ranges come out of the key sort's last pass)
     BlendArgs ba{};
     ba.splats = e->d_splats;
     ba.n = e->n;

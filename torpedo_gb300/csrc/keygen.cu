@@ -1,7 +1,8 @@
-// keygen.cu — kernel (b, second half): key duplication, and kernel (d): tile ranges.
+// keygen.cu — kernel (b, second half): key duplication.
 //
 // Reference: keygen.slang:23-53 (one thread per Gaussian looping over its tile
-// rect) and range.slang:18-35 (+ fillBuffer, GaussianEngine.cpp:843-848).
+// rect). It also presets the tile ranges (fillBuffer, GaussianEngine.cpp:843-848)
+// that the key sort's last pass fills in (range.slang:18-35, in sort.cu).
 //
 // GB300 form of keygen: Gaussians are visited in depth order (a prior sort of
 // the (view | depth) keys), so the emitted keys only need a stable sort on
@@ -54,7 +55,8 @@ __global__ void __launch_bounds__(kKeygenThreads)
     keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
                   const uint32_t* __restrict__ offsets, uint32_t count, uint32_t n,
                   const ViewConst* __restrict__ views, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                  uint32_t capacity, uint32_t key_bits, FrameCtl* ctl) {
+                  uint32_t capacity, uint32_t key_bits, uint32_t* __restrict__ ranges, uint32_t n_tiles,
+                  FrameCtl* ctl) {
     __shared__ KeygenSmem S;
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     const uint32_t warps_total = (gridDim.x * blockDim.x) >> 5;
@@ -62,6 +64,9 @@ __global__ void __launch_bounds__(kKeygenThreads)
     if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
     if (ctl->status & kStatusFatal) return;
     const uint32_t npass = min(8u, (key_bits + 7) / 8);
+    // ranges: (0xFFFFFFFF, 0) until the key sort's last pass narrows them
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x)
+        reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0xFFFFFFFFu, 0u);
     for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x) (&S.hist[0][0])[k] = 0;
     __syncthreads();
     uint64_t* wkeys = S.keys[warp];
@@ -159,34 +164,11 @@ __global__ void __launch_bounds__(kKeygenThreads)
             if (S.hist[p - 4][d]) atomicAdd(&ctl->sort_hist[p][d], S.hist[p - 4][d]);
 }
 
-// range.slang:18-35 over K = min(total_keys, capacity) keys; ranges zeroed first.
-__global__ void tile_ranges_kernel(const uint64_t* __restrict__ keys, uint32_t* __restrict__ ranges,
-                                   uint32_t n_tiles, FrameCtl* ctl, uint32_t capacity) {
-    if (ctl->status & kStatusFatal) return;
-    const uint32_t K = min(ctl->total_keys, capacity);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < K; idx += stride) {
-        if (!TPD_INBOUNDS(ctl, 30, idx, capacity)) continue;
-        const uint32_t cur = uint32_t(keys[idx] >> 32);
-        if (cur >= n_tiles) continue;  // only reachable with corrupted keys
-        if (idx == 0) {
-            ranges[cur * 2 + 0] = 0;
-        } else {
-            const uint32_t prev = uint32_t(keys[idx - 1] >> 32);
-            if (cur != prev && TPD_INBOUNDS(ctl, 31, cur, n_tiles)) {
-                if (prev < n_tiles) ranges[prev * 2 + 1] = idx;
-                ranges[cur * 2 + 0] = idx;
-            }
-        }
-        if (idx == K - 1) ranges[cur * 2 + 1] = idx + 1;
-    }
-}
-
 }  // namespace
 
 void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t count, uint32_t n,
                    const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
-                   FrameCtl* ctl, int num_sms, cudaStream_t s) {
+                   uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s) {
     if (count == 0 || n == 0) return;
     const uint64_t warps = (uint64_t(count) + 31) / 32;
     uint64_t blocks = (warps * 32 + kKeygenThreads - 1) / kKeygenThreads;
@@ -199,14 +181,8 @@ void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* o
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
     blocks = blocks < cap ? blocks : cap;
     keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, count, n, views, keys, vals,
-                                                              capacity, key_bits, ctl);
+                                                              capacity, key_bits, ranges, n_tiles, ctl);
 }
 
-void launch_tile_ranges(const uint64_t* keys, uint32_t n_tiles, uint32_t* ranges, FrameCtl* ctl, uint32_t capacity,
-                        int num_sms, cudaStream_t s) {
-    cudaMemsetAsync(ranges, 0, size_t(n_tiles) * 8, s);
-    const int blocks = (num_sms > 0 ? num_sms : 148) * 8;
-    tile_ranges_kernel<<<blocks, 256, 0, s>>>(keys, ranges, n_tiles, ctl, capacity);
-}
 
 }  // namespace tpd

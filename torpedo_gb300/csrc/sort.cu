@@ -177,6 +177,32 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
     return excl;
 }
 
+// Tile ranges (range.slang:18-35) from the last pass of the key sort: the
+// partition's keys sit in shared memory fully sorted within each digit run,
+// and a digit run is contiguous in the output. A tile starts where the run's
+// previous key has another tile and ends where the next one has; at the
+// edges of a run the neighbour lies in another partition, and min / max
+// reductions over all candidates give the range whatever the order.
+template <int kItems, int kThreads>
+__device__ __forceinline__ void tile_range_bounds(const OnesweepSmem<kItems, kThreads>& S, uint32_t* ranges,
+                                                  uint32_t n_tiles, uint64_t key, uint32_t j, uint32_t cnt,
+                                                  uint32_t d, uint32_t g, uint32_t shift, uint32_t mask,
+                                                  FrameCtl* ctl) {
+    const uint32_t t = uint32_t(key >> 32);
+    if (!TPD_INBOUNDS(ctl, 18, t, n_tiles)) return;
+    bool first = j == 0, last = j + 1 == cnt;
+    if (!first) {
+        const uint64_t kp = S.keys[pad16(j - 1)];
+        first = (uint32_t(kp >> shift) & mask) != d || uint32_t(kp >> 32) != t;
+    }
+    if (!last) {
+        const uint64_t kn = S.keys[pad16(j + 1)];
+        last = (uint32_t(kn >> shift) & mask) != d || uint32_t(kn >> 32) != t;
+    }
+    if (first) atomicMin(&ranges[2 * t], g);
+    if (last) atomicMax(&ranges[2 * t + 1], g + 1);
+}
+
 // kThreads = 256 (one digit per thread) or 512 (the digit-wide steps run on
 // the first 256 threads); a partition is kThreads * kItems keys.
 template <int kItems, int kThreads, int kMinBlocks>
@@ -185,7 +211,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
                     uint32_t pass, uint32_t shift, uint32_t bits, const uint32_t (*hist)[256], uint32_t ticket_slot,
                     uint32_t tag_slot, uint32_t fixed_count, uint64_t* __restrict__ desc, FrameCtl* ctl,
-                    uint32_t spin_limit) {
+                    uint32_t spin_limit, uint32_t* __restrict__ ranges, uint32_t n_tiles) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr uint32_t kSortItems = kItems, kSortTile = kThreads * kItems, kWarps = kThreads / 32;
     OnesweepSmem<kItems, kThreads>& S = *reinterpret_cast<OnesweepSmem<kItems, kThreads>*>(smem_raw);
@@ -322,6 +348,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             if (g < capacity && TPD_INBOUNDS(ctl, 17, g, K + (K == 0))) {
                 keys_out[g] = key;
                 vals_out[g] = S.vals[pad16(j)];
+                if (ranges) tile_range_bounds(S, ranges, n_tiles, key, j, cnt, d, g, shift, mask, ctl);
             }
         }
         __syncthreads();  // S.keys / S.vals / S.gmap are rewritten by the next partition
@@ -361,7 +388,7 @@ void launch_passes(uint64_t* kin, uint32_t* vin, uint64_t* kout, uint32_t* vout,
         const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
         onesweep_kernel<kItems, kThreads, kMinBlocks><<<grid, kThreads, smem, s>>>(
             kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p, plan.tag_base + p,
-            plan.fixed_count, desc, ctl, spin_limit);
+            plan.fixed_count, desc, ctl, spin_limit, p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

@@ -77,9 +77,10 @@ void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint6
 // index, for the items[] in depth order with their key offsets. K is read from
 // ctl->total_keys; keys beyond capacity are dropped and flagged. Also counts the
 // digits of the tile-id passes (digit positions 4.. of key_bits) into ctl->sort_hist.
+// Also presets ranges (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
 void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t count, uint32_t n,
                    const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
-                   FrameCtl* ctl, int num_sms, cudaStream_t s);
+                   uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s);
 
 // Onesweep LSD radix sort of (key, val) pairs on key bits [first_bit, key_bits),
 // first_bit a multiple of 8. K = min(ctl->total_keys, capacity). hist: the
@@ -100,6 +101,8 @@ struct SortPlan {
     int ctas_per_sm = 2;
     uint32_t items = 16;               // keys per thread: 16 (4096-key partitions), 8 or 4
     uint32_t threads = 256;            // 512: 4096-key partitions as 512 threads x 8 keys (items 16 only)
+    uint32_t* ranges = nullptr;        // key sort: the last pass also writes the tile ranges (preset by keygen)
+    uint32_t n_tiles = 0;
     uint32_t fixed_count = 0;          // nonzero: sort this many pairs, else min(ctl->total_keys, capacity)
     cudaEvent_t after_hist = nullptr;  // recorded between the histogram and the first pass
 };
@@ -110,9 +113,6 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
 // (standalone stage calls).
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s);
 
-// range.slang: ranges[tile] = [start, end) over sorted keys, zero elsewhere.
-void launch_tile_ranges(const uint64_t* keys, uint32_t n_tiles, uint32_t* ranges, FrameCtl* ctl, uint32_t capacity,
-                        int num_sms, cudaStream_t s);
 
 struct BlendArgs {
     const Splat* splats;      // n_views x n (view-major)
@@ -120,7 +120,7 @@ struct BlendArgs {
     FrameCtl* ctl;            // K = min(ctl->total_keys, capacity); frames with a fatal status are skipped
     uint32_t capacity;
     const uint32_t* vals;
-    const uint32_t* ranges;   // 2 x n_tiles (global tile ids)
+    uint32_t* ranges;         // 2 x n_tiles (global tile ids); an empty tile's (0xFFFFFFFF, 0) is rewritten to (0, 0)
     const ViewConst* views;   // device, n_views entries
     const uint32_t* tile_view;  // per global tile: view index (nullptr: single view 0)
     uint32_t n_tiles;
