@@ -8,10 +8,11 @@
 // the (view | depth) keys), so the emitted keys only need a stable sort on
 // their tile-id bits afterwards: per tile the order is (depth, index), exactly
 // the reference's stable sort of (tile | depth) keys emitted in index order.
-// A warp owns 32 consecutive Gaussians and builds their (contiguous) keys in
-// a shared-memory window: small Gaussians one lane each, large ones by the
-// whole warp, so one large Gaussian does not serialise its warp; each window
-// is stored coalesced. Keys and values are bit-identical to the reference's.
+// A warp owns 32 consecutive Gaussians and writes their (contiguous) keys
+// one output slot per lane, finding each slot's Gaussian through a small
+// owner map in shared memory, so stores are coalesced and one large Gaussian
+// does not serialise its warp. Keys and values are bit-identical to the
+// reference's.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 #include "tpd_scan.cuh"
@@ -23,33 +24,30 @@ constexpr uint32_t kKeygenThreads = 256;
 
 // Walks the (view, Gaussian) items in depth order (items[r] = v * n + i, their
 // key offsets in offsets[r]); a warp owns 32 consecutive items, whose keys
-// are contiguous. The warp builds its keys in windows of kKeyWindow slots of
-// shared memory and copies each window out coalesced:
-//  - a Gaussian with at most kSmallKeys keys is expanded by its own lane,
-//    stepping through its rectangle row-major without any division;
-//  - a larger one is expanded by the whole warp, one slot per lane.
+// are contiguous, and produces them in windows of kKeyWindow output slots:
+//  1. each lane with keys marks its first slot in the window's owner map,
+//     a prefix-max over the map gives every slot its owning lane;
+//  2. lane l fills slots l, l + 32, ...: owner's rectangle from a per-warp
+//     table, (row, column) of the slot's index inside the rectangle, the key,
+//     one coalesced store of key and value.
 // Besides the keys it counts the digits of the tile-id passes (digit
-// positions 4.. of key_bits) into ctl->sort_hist, one shared-memory atomic
-// per key and pass (the lanes of a step work on different Gaussians, so they
-// rarely collide); the low 32 bits of a key are its depth, already ordered,
-// so no depth digit is counted or sorted. Keys past the capacity are neither
-// written nor counted.
+// positions 4.. of key_bits) into ctl->sort_hist: lanes of a store group hold
+// consecutive keys, so equal digits come in runs of neighbouring lanes and
+// each run adds its length with one shared-memory atomic. The low 32 bits of
+// a key are its depth, already ordered, so no depth digit is counted or
+// sorted. Keys past the capacity are neither written nor counted.
 constexpr uint32_t kKeyWindow = 256;
-constexpr uint32_t kSmallKeys = 32;
 constexpr uint32_t kKeygenWarps = kKeygenThreads / 32;
 
 struct KeygenSmem {
-    uint64_t keys[kKeygenWarps][kKeyWindow];
-    uint32_t vals[kKeygenWarps][kKeyWindow];
-    uint32_t hist[4][256];  // tile-id digit positions 4..7
+    uint32_t owner[kKeygenWarps][kKeyWindow];  // owning lane of each slot of the window
+    uint32_t t0[kKeygenWarps][32];             // first tile of the lane's rectangle
+    uint32_t wgx[kKeygenWarps][32];            // rectangle width | view grid width << 16
+    uint32_t excl[kKeygenWarps][32];           // first slot of the lane's keys (warp-relative)
+    uint32_t db[kKeygenWarps][32];             // depth bits
+    uint32_t gi[kKeygenWarps][32];             // Gaussian index
+    uint32_t hist[4][256];                     // tile-id digit positions 4..7
 };
-
-__device__ __forceinline__ void count_tile(KeygenSmem& S, uint32_t tile, uint32_t npass, uint32_t key_bits) {
-    for (uint32_t p = 4; p < npass; ++p) {
-        const uint32_t mask = (1u << min(8u, key_bits - 8u * p)) - 1u;
-        atomicAdd(&S.hist[p - 4][(tile >> (8u * (p - 4))) & mask], 1u);
-    }
-}
 
 __global__ void __launch_bounds__(kKeygenThreads)
     keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
@@ -69,13 +67,13 @@ __global__ void __launch_bounds__(kKeygenThreads)
         reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0xFFFFFFFFu, 0u);
     for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x) (&S.hist[0][0])[k] = 0;
     __syncthreads();
-    uint64_t* wkeys = S.keys[warp];
-    uint32_t* wvals = S.vals[warp];
+    uint32_t* owner = S.owner[warp];
     const uint32_t nwarps = (count + 31) / 32;
+    const uint32_t lt = (1u << lane) - 1u;
 
     for (uint32_t wi = warp_global; wi < nwarps; wi += warps_total) {
         const uint32_t r = wi * 32u + lane;
-        // per item: first tile (row-major in its view), rect width, view grid width
+        // per item: first tile (row-major in its view), rect width and height, view grid width
         uint32_t w = 1, h = 0, gx = 1, off = 0, depth_bits = 0, gi = 0, t0 = 0;
         if (r < count) {
             const uint32_t item = items[r];
@@ -103,60 +101,81 @@ __global__ void __launch_bounds__(kKeygenThreads)
         const uint32_t excl = incl - cnt;
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
         const uint32_t base = __shfl_sync(0xFFFFFFFFu, off, 0);
-        const uint32_t big_lanes = __ballot_sync(0xFFFFFFFFu, cnt > kSmallKeys);
+        S.t0[warp][lane] = t0;
+        S.wgx[warp][lane] = w | (gx << 16);
+        S.excl[warp][lane] = excl;
+        S.db[warp][lane] = depth_bits;
+        S.gi[warp][lane] = gi;
 
         for (uint32_t c0 = 0; c0 < total; c0 += kKeyWindow) {
-            const uint32_t c1 = min(total, c0 + kKeyWindow);
-            // small Gaussians: each lane writes its own slots of the window
-            if (cnt <= kSmallKeys) {
-                const uint32_t lo = max(excl, c0), hi = min(excl + cnt, c1);
-                if (lo < hi) {
-                    const uint32_t local = lo - excl;
-                    uint32_t ty = local / w, tx = local - ty * w;
-                    uint32_t tile = t0 + ty * gx + tx;
-                    for (uint32_t k = lo; k < hi; ++k) {
-                        wkeys[k - c0] = (uint64_t(tile) << 32) | depth_bits;
-                        wvals[k - c0] = gi;
-                        if (uint64_t(base) + k < capacity) count_tile(S, tile, npass, key_bits);
-                        if (++tx == w) {  // next row of the rectangle
-                            tx = 0;
-                            tile += gx - w + 1;
-                        } else {
-                            ++tile;
-                        }
+            const uint32_t span = min(kKeyWindow, total - c0);
+            // 1. owner map: segment starts, then a prefix max over the window
+            //    (owners grow with the slot; slot c0 belongs to the last lane
+            //    whose keys start at or before it)
+#pragma unroll
+            for (uint32_t q = 0; q < kKeyWindow / 32; ++q) owner[lane * (kKeyWindow / 32) + q] = 0;
+            __syncwarp();
+            if (cnt && excl >= c0 && excl < c0 + kKeyWindow) owner[excl - c0] = lane;
+            const uint32_t first_owner = 31u - __clz(__ballot_sync(0xFFFFFFFFu, excl <= c0 && cnt));
+            __syncwarp();
+            uint32_t run = 0, mine[kKeyWindow / 32];
+#pragma unroll
+            for (uint32_t q = 0; q < kKeyWindow / 32; ++q) {
+                run = max(run, owner[lane * (kKeyWindow / 32) + q]);
+                mine[q] = run;
+            }
+            uint32_t before = run;  // exclusive prefix max of the lanes' maxima
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, before, o);
+                if (lane >= o) before = max(before, x);
+            }
+            before = __shfl_up_sync(0xFFFFFFFFu, before, 1);
+            before = max(lane ? before : 0u, first_owner);
+            __syncwarp();
+#pragma unroll
+            for (uint32_t q = 0; q < kKeyWindow / 32; ++q) owner[lane * (kKeyWindow / 32) + q] = max(before, mine[q]);
+            __syncwarp();
+            // 2. slots lane, lane + 32, ...: one coalesced store group per step
+            for (uint32_t q = lane; q - lane < span; q += 32u) {
+                const bool live = q < span && uint64_t(base) + c0 + q < capacity;
+                uint32_t tile = 0;
+                if (live) {
+                    const uint32_t j = owner[q];
+                    const uint32_t local = c0 + q - S.excl[warp][j];  // < 2^24: exact in a float
+                    const uint32_t jwg = S.wgx[warp][j];
+                    const uint32_t jw = jwg & 0xFFFFu;
+                    // row = local / jw from a float quotient, corrected by one step
+                    uint32_t ty = __float2uint_rz(__fdividef(float(local), float(jw)));
+                    int32_t rem = int32_t(local) - int32_t(ty * jw);
+                    if (rem < 0) {
+                        --ty;
+                        rem += int32_t(jw);
+                    } else if (rem >= int32_t(jw)) {
+                        ++ty;
+                        rem -= int32_t(jw);
+                    }
+                    tile = S.t0[warp][j] + ty * (jwg >> 16) + uint32_t(rem);
+                    const uint64_t pos = uint64_t(base) + c0 + q;
+                    keys[pos] = (uint64_t(tile) << 32) | S.db[warp][j];
+                    vals[pos] = S.gi[warp][j];
+                }
+                // digits: runs of equal digits among neighbouring lanes, one atomic per run
+                const uint32_t live_mask = __ballot_sync(0xFFFFFFFFu, live);
+                for (uint32_t p = 4; p < npass; ++p) {
+                    const uint32_t d = (tile >> (8u * (p - 4))) & ((1u << min(8u, key_bits - 8u * p)) - 1u);
+                    const uint32_t dprev = __shfl_up_sync(0xFFFFFFFFu, d, 1);
+                    const uint32_t starts = __ballot_sync(0xFFFFFFFFu, live && (lane == 0 || dprev != d)) & live_mask;
+                    if (live && ((starts >> lane) & 1u)) {
+                        const uint32_t later = starts & ~(lt | (1u << lane));  // run starts after this lane
+                        const uint32_t stop = later ? uint32_t(__ffs(later) - 1) : 32u - __clz(live_mask);
+                        atomicAdd(&S.hist[p - 4][d], stop - lane);
                     }
                 }
             }
-            // large Gaussians: the whole warp, one slot per lane
-            for (uint32_t bm = big_lanes; bm; bm &= bm - 1u) {
-                const uint32_t j = uint32_t(__ffs(bm) - 1);
-                const uint32_t jex = __shfl_sync(0xFFFFFFFFu, excl, j);
-                const uint32_t jcnt = __shfl_sync(0xFFFFFFFFu, cnt, j);
-                const uint32_t jt0 = __shfl_sync(0xFFFFFFFFu, t0, j);
-                const uint32_t jw = __shfl_sync(0xFFFFFFFFu, w, j);
-                const uint32_t jgx = __shfl_sync(0xFFFFFFFFu, gx, j);
-                const uint32_t jdb = __shfl_sync(0xFFFFFFFFu, depth_bits, j);
-                const uint32_t jgi = __shfl_sync(0xFFFFFFFFu, gi, j);
-                const uint32_t lo = max(jex, c0), hi = min(jex + jcnt, c1);
-                for (uint32_t k = lo + lane; k < hi; k += 32u) {
-                    const uint32_t local = k - jex;
-                    const uint32_t ty = local / jw;
-                    const uint32_t tile = jt0 + ty * jgx + (local - ty * jw);
-                    wkeys[k - c0] = (uint64_t(tile) << 32) | jdb;
-                    wvals[k - c0] = jgi;
-                    if (uint64_t(base) + k < capacity) count_tile(S, tile, npass, key_bits);
-                }
-            }
-            __syncwarp();
-            for (uint32_t q = lane; q < c1 - c0; q += 32u) {
-                const uint64_t pos = uint64_t(base) + c0 + q;
-                if (pos < capacity) {
-                    keys[pos] = wkeys[q];
-                    vals[pos] = wvals[q];
-                }
-            }
-            __syncwarp();  // the window is refilled next
+            __syncwarp();  // the owner map is rebuilt for the next window
         }
+        __syncwarp();  // the lane table is rewritten by the next items
     }
     __syncthreads();
     for (uint32_t p = 4; p < npass; ++p)
