@@ -222,9 +222,10 @@ def general_sort(eng, K, key_bits, stream, steps):
 
 def kernels_per_frame(views: int, tile_passes: int) -> int:
     """Kernel launches of one frame: frame_begin, preprocess, depth-sort passes,
-    depth-order scan, keygen, tile-id sort passes, ranges, blend."""
+    depth-order scan, keygen, tile-id sort passes (the last one also writes the
+    tile ranges), blend."""
     depth_passes = math.ceil((32 + (views - 1).bit_length()) / 8)
-    return 6 + depth_passes + tile_passes
+    return 5 + depth_passes + tile_passes
 
 
 def _params(sc, dev):

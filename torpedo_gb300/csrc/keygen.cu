@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
             const uint32_t item = items[r];
             off = offsets[r];
             if (TPD_INBOUNDS(ctl, 21, item, count)) {
-                const uint32_t v = item / n;
+                const uint32_t v = count == n ? 0u : item / n;  // one view: no division
                 gi = item - v * n;
                 const ViewConst& vc = views[v];
                 gx = grid_x(vc.width);

@@ -134,13 +134,16 @@ __device__ __forceinline__ int trunc_to_int(float v) { return __float2int_rz(v);
 
 // getBoundingRect (splat/volume.slang:12-17). Same float operations as the shader:
 // ((p - r) / 16) and ((p + r) + 15) / 16, truncated toward zero, clamped to the grid.
+// Dividing by 16 is multiplying by 2^-4: both round the same exact quotient,
+// so the product gives the division's result bit for bit.
+static_assert(kBlockX == 16, "the tile rect divides by 16 as a multiply by 2^-4");
 __device__ __forceinline__ void bounding_rect(float px, float py, float radius, uint32_t gx, uint32_t gy,
                                               uint32_t& x0, uint32_t& y0, uint32_t& x1, uint32_t& y1) {
-    const float bx = float(kBlockX), b1 = float(kBlockX - 1);
-    const int a = trunc_to_int(__fdiv_rn(__fsub_rn(px, radius), bx));
-    const int b = trunc_to_int(__fdiv_rn(__fsub_rn(py, radius), bx));
-    const int c = trunc_to_int(__fdiv_rn(__fadd_rn(__fadd_rn(px, radius), b1), bx));
-    const int d = trunc_to_int(__fdiv_rn(__fadd_rn(__fadd_rn(py, radius), b1), bx));
+    const float inv = 0.0625f, b1 = float(kBlockX - 1);
+    const int a = trunc_to_int(__fmul_rn(__fsub_rn(px, radius), inv));
+    const int b = trunc_to_int(__fmul_rn(__fsub_rn(py, radius), inv));
+    const int c = trunc_to_int(__fmul_rn(__fadd_rn(__fadd_rn(px, radius), b1), inv));
+    const int d = trunc_to_int(__fmul_rn(__fadd_rn(__fadd_rn(py, radius), b1), inv));
     x0 = min(gx, uint32_t(max(0, a)));
     y0 = min(gy, uint32_t(max(0, b)));
     x1 = min(gx, uint32_t(max(0, c)));
