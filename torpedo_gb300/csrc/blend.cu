@@ -155,11 +155,29 @@ __device__ __forceinline__ void load_view_tile(const BlendArgs* /*unused*/, cons
     ty = local / gx;
 }
 
+// Stages list entry j (of the tile's [start, end)) into slot tid of buffer b.
+struct BlendStage {
+    float2 xy[2][kBlendThreads];
+    float4 q[2][kBlendThreads];
+    float4 col[2][kBlendThreads];
+    float4 box[2][kBlendThreads];
+};
+
+__device__ __forceinline__ void stage_slot(BlendStage& S, uint32_t b, uint32_t tid, uint32_t j, const BlendArgs& a,
+                                           const Splat* vsplats) {
+    if (!TPD_INBOUNDS(a.ctl, 40, j, a.capacity)) return;
+    const uint32_t idx = a.vals[j];
+    if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n))
+        stage_entry(vsplats + idx, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);
+    else
+        stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);  // only reachable with corrupted lists
+}
+
+// Rounds of 256 list entries, double-buffered: while the warps walk round r,
+// each thread stages its entry of round r + 1 into the other buffer, and one
+// barrier per round (which also counts finished pixels) separates the two.
 __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
-    __shared__ float2 s_xy[kBlendThreads];
-    __shared__ float4 s_q[kBlendThreads];
-    __shared__ float4 s_col[kBlendThreads];
-    __shared__ float4 s_box[kBlendThreads];
+    __shared__ BlendStage S;
 
     const uint32_t tile = blockIdx.x;
     // an overflowed frame is re-rendered with larger key buffers; nothing to draw
@@ -184,23 +202,20 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     bool done = !inside;
     float T = 1.0f, C0 = 0.f, C1 = 0.f, C2 = 0.f;
     uint32_t last = 0;
-    for (uint32_t b0 = start; b0 < end; b0 += kBlendThreads) {
-        if (__syncthreads_count(done) == kBlendThreads) break;
-        const uint32_t j = b0 + tid;
-        if (j < end && TPD_INBOUNDS(a.ctl, 40, j, a.capacity)) {
-            const uint32_t idx = a.vals[j];
-            if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n))
-                stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);
-            else
-                stage_empty(s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);  // only reachable with corrupted lists
-        }
-        __syncthreads();
+    if (start < end && start + tid < end) stage_slot(S, 0, tid, start + tid, a, vsplats);
+    bool all_done = __syncthreads_count(done) == kBlendThreads;
+    uint32_t r = 0;
+    for (uint32_t b0 = start; b0 < end && !all_done; b0 += kBlendThreads, ++r) {
+        const uint32_t b = r & 1u;
+        // the next round's entry, into the buffer the last barrier released
+        if (b0 + kBlendThreads + tid < end) stage_slot(S, b ^ 1u, tid, b0 + kBlendThreads + tid, a, vsplats);
         const uint32_t n = min(kBlendThreads, end - b0);
         if (!TPD_INBOUNDS(a.ctl, 43, n, kBlendThreads + 1)) break;
         for (uint32_t g = 0; g < n; g += 32) {
             if (__all_sync(0xFFFFFFFFu, done)) break;
             const uint32_t e = g + lane;
-            uint32_t m = __ballot_sync(0xFFFFFFFFu, e < n && entry_meets_block(s_xy[e], s_q[e], s_box[e], bxf, byf));
+            uint32_t m = __ballot_sync(0xFFFFFFFFu,
+                                       e < n && entry_meets_block(S.xy[b][e], S.q[b][e], S.box[b][e], bxf, byf));
             // branch-free body: every lane evaluates the pair and selects the
             // update, so a warp whose lanes take different decisions does not
             // run the paths one after another
@@ -208,9 +223,9 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
                 const uint32_t jj = g + uint32_t(__ffs(m) - 1);
                 m &= m - 1u;
                 float dx, dy;
-                const float4 q = s_q[jj];
-                const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
-                const float4 col = s_col[jj];
+                const float4 q = S.q[b][jj];
+                const float p2 = pair_p2(S.xy[b][jj], q, pxf, pyf, dx, dy);
+                const float4 col = S.col[b][jj];
                 const float alpha = fminf(kAlphaMax, __fmul_rn(col.w, ex2_approx(p2)));
                 const float tn = __fmul_rn(T, __fsub_rn(1.0f, alpha));
                 const bool live = !done && !pair_skipped(p2, q.w);
@@ -225,6 +240,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
                 last = add ? b0 + jj - start + 1 : last;
             }
         }
+        all_done = __syncthreads_count(done) == kBlendThreads;
     }
     if (inside && TPD_INBOUNDS(a.ctl, 41, tile, a.n_tiles)) {
         const size_t p = (a.image_offset ? a.image_offset[vi] : 0ull) + size_t(pyl) * W + pxl;
