@@ -309,16 +309,18 @@ def plain_views_rate(cfg_name, local, passes, settings):
                 e.backward(d, *grads)
 
         one_pass()  # warm-up: sizes the key buffers of every engine
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        for _ in range(passes):
+        best = None
+        for _ in range(passes):  # the fastest pass: host round trips make single passes noisy
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
             one_pass()
-        torch.cuda.synchronize(dev)
-        dt = time.perf_counter() - t0
+            torch.cuda.synchronize(dev)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
     finally:
         for e in engines.values():
             e.close()
-    return passes * len(cams) / dt
+    return len(cams) / best
 
 
 def run_train_only(args):
@@ -474,13 +476,14 @@ def run_ours(args):
                    "step": "forward frame + backward to means, log-scales, quaternions, opacity logits, SH; "
                            "one captured CUDA graph per step"}
         ms3, st3, views3, pixels3 = train_rate("cfg3", stream, local, 5, 2, settings)
-        plain = plain_views_rate("cfg3", local, 1, settings)
+        plain = plain_views_rate("cfg3", local, 3, settings)
         batched = {"config": "cfg3: 500,000 Gaussians (means N(0,1)^3), 64 views on a sphere of radius 5, sizes "
                              "from {640x480, 1280x720, 1920x1080} (seed 3), dL/dimage ~ N(0,1)",
                    "views_per_s": round(views3 * 1000.0 / ms3, 2), "ms_per_step": round(ms3, 3),
                    "keys": int(st3["keys"]), "pixels": pixels3,
                    "plain_views_per_s": round(plain, 2), "batched_over_plain": round(views3 * 1000.0 / ms3 / plain, 3),
-                   "plain": "one view per call: set_camera, raster_frame, backward, each waiting for its work"}
+                   "plain": "one view per call: set_camera, raster_frame, backward, each waiting for its work; "
+                            "fastest of 3 passes over the 64 views"}
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -301,13 +301,25 @@ __device__ __forceinline__ float warp_sum8_transposed(const float (&v)[8], uint3
     return c;
 }
 
+// Rounds of 256 list entries from the back, as in the forward: staging
+// double-buffered, per-round gradient sums in one of two shared buffers. The
+// barrier at the end of a round completes its sums; each thread then adds its
+// share of them to global memory and zeroes what it added, so the buffer is
+// clean when it comes round again two rounds later. The staged indices that
+// the flush reads live in three buffers (the next round's staging overwrites
+// the one of the round before the last).
+struct BlendBackwardSmem {
+    BlendStage stage;
+    float acc[2][kBlendThreads][kG2DStride];
+    uint32_t idx[3][kBlendThreads];
+};
+
 __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBackwardArgs a) {
-    __shared__ float2 s_xy[kBlendThreads];
-    __shared__ float4 s_q[kBlendThreads];
-    __shared__ float4 s_col[kBlendThreads];
-    __shared__ float4 s_box[kBlendThreads];
-    __shared__ uint32_t s_idx[kBlendThreads];
-    __shared__ __align__(16) float s_acc[kBlendThreads][kG2DStride];
+    extern __shared__ __align__(16) unsigned char bwd_smem[];
+    BlendBackwardSmem& SM = *reinterpret_cast<BlendBackwardSmem*>(bwd_smem);
+    BlendStage& S = SM.stage;
+    auto& s_idx = SM.idx;
+    auto& s_acc = SM.acc;
 
     const uint32_t tile = blockIdx.x;
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
@@ -348,29 +360,36 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
 
     float S0 = 0.f, S1 = 0.f, S2 = 0.f;  // colour accumulated behind the current entry
     float* g2d_view = a.g2d + size_t(vi) * a.g2d_view_stride;
-    for (int32_t r_end = int32_t(max_last); r_end > 0; r_end -= int32_t(kBlendThreads)) {
-        const int32_t r0 = max(0, r_end - int32_t(kBlendThreads));
-        const uint32_t n = uint32_t(r_end - r0);
-        __syncthreads();
+    // stages the round whose list positions (relative) end at r_end: entry
+    // tid is position r_end - 1 - tid
+    auto stage_round = [&](int32_t r_end, uint32_t b, uint32_t bi) {
+        const uint32_t n = uint32_t(min(int32_t(kBlendThreads), r_end));
         if (tid < n) {
-            const uint32_t e = uint32_t(r_end) - 1u - tid;  // descending list position (relative)
+            const uint32_t e = uint32_t(r_end) - 1u - tid;
             uint32_t idx = a.vals[start + e];
             if (idx < a.n) {
-                stage_entry(vsplats + idx, s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);
+                stage_entry(vsplats + idx, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);
             } else {  // only reachable with corrupted lists
                 idx = 0;
-                stage_empty(s_xy[tid], s_q[tid], s_col[tid], s_box[tid]);
+                stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);
             }
-            s_idx[tid] = idx;
+            s_idx[bi][tid] = idx;
         }
-        for (uint32_t k = tid; k < n * kG2DStride; k += kBlendThreads) (&s_acc[0][0])[k] = 0.f;
-        __syncthreads();
+    };
+    for (uint32_t k = tid; k < 2 * kBlendThreads * kG2DStride; k += kBlendThreads) (&s_acc[0][0][0])[k] = 0.f;
+    if (max_last > 0) stage_round(int32_t(max_last), 0, 0);
+    __syncthreads();
+    uint32_t r = 0;
+    for (int32_t r_end = int32_t(max_last); r_end > 0; r_end -= int32_t(kBlendThreads), ++r) {
+        const uint32_t b = r & 1u, bi = r % 3u;
+        const uint32_t n = uint32_t(min(int32_t(kBlendThreads), r_end));
+        if (r_end > int32_t(kBlendThreads)) stage_round(r_end - int32_t(kBlendThreads), b ^ 1u, (r + 1) % 3u);
         // entries jj >= skip have list positions r_end - 1 - jj below warp_last
         const uint32_t skip = uint32_t(r_end) > warp_last ? uint32_t(r_end) - warp_last : 0u;
         for (uint32_t g = skip & ~31u; g < n; g += 32) {
             const uint32_t jl = g + lane;
             uint32_t m = __ballot_sync(0xFFFFFFFFu, jl < n && jl >= skip &&
-                                                        entry_meets_block(s_xy[jl], s_q[jl], s_box[jl], bxf, byf));
+                                                        entry_meets_block(S.xy[b][jl], S.q[b][jl], S.box[b][jl], bxf, byf));
             while (m) {
                 const uint32_t jj = g + uint32_t(__ffs(m) - 1);
                 m &= m - 1u;
@@ -378,9 +397,9 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
                 // branch-free body (as in the forward): every lane evaluates,
                 // the selects keep only contributing pairs
                 float dx, dy;
-                const float4 q = s_q[jj];
-                const float p2 = pair_p2(s_xy[jj], q, pxf, pyf, dx, dy);
-                const float4 col = s_col[jj];
+                const float4 q = S.q[b][jj];
+                const float p2 = pair_p2(S.xy[b][jj], q, pxf, pyf, dx, dy);
+                const float4 col = S.col[b][jj];
                 const bool contrib = inside && e < last && !pair_skipped(p2, q.w);
                 const float G = ex2_approx(p2);
                 const float raw = __fmul_rn(col.w, G);
@@ -409,22 +428,26 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
                 gv[8] = contrib ? g2 * w : 0.0f;
                 if (__any_sync(0xFFFFFFFFu, contrib)) {
                     const float lo[8] = {gv[0], gv[1], gv[2], gv[3], gv[4], gv[5], gv[6], gv[7]};
-                    const float r = warp_sum8_transposed(lo, lane);
-                    float b = gv[8];
+                    const float rs = warp_sum8_transposed(lo, lane);
+                    float b9 = gv[8];
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
-                    if ((lane & 3u) == 0) atomicAdd(&s_acc[jj][lane >> 2], r);
-                    if (lane == 0) atomicAdd(&s_acc[jj][8], b);
+                    for (int o = 16; o > 0; o >>= 1) b9 += __shfl_xor_sync(0xFFFFFFFFu, b9, o);
+                    if ((lane & 3u) == 0) atomicAdd(&s_acc[b][jj][lane >> 2], rs);
+                    if (lane == 0) atomicAdd(&s_acc[b][jj][8], b9);
                 }
             }
         }
-        __syncthreads();
-        // one 16-byte vector atomic per non-zero quarter of an entry's record
+        __syncthreads();  // round r's sums complete; the other stage buffer is filled
+        // one 16-byte vector atomic per non-zero quarter of an entry's record;
+        // the thread that adds a quarter also zeroes it for round r + 2
         for (uint32_t k = tid; k < n * 3; k += kBlendThreads) {
             const uint32_t jj = k / 3, c = k % 3;
-            const float4 v = reinterpret_cast<const float4*>(&s_acc[jj][0])[c];
-            if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f)
-                atomicAdd(reinterpret_cast<float4*>(g2d_view + size_t(s_idx[jj]) * kG2DStride) + c, v);
+            float4* slot = reinterpret_cast<float4*>(&s_acc[b][jj][0]) + c;
+            const float4 v = *slot;
+            if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f) {
+                atomicAdd(reinterpret_cast<float4*>(g2d_view + size_t(s_idx[bi][jj]) * kG2DStride) + c, v);
+                *slot = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         }
     }
 }
@@ -443,7 +466,13 @@ void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStre
 
 void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s) {
     if (a.n_tiles == 0) return;
-    blend_backward_kernel<<<a.n_tiles, kBlendThreads, 0, s>>>(a);
+    static bool configured = false;  // more than 48 KB of shared memory needs the opt-in
+    if (!configured) {
+        cudaFuncSetAttribute(blend_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(sizeof(BlendBackwardSmem)));
+        configured = true;
+    }
+    blend_backward_kernel<<<a.n_tiles, kBlendThreads, sizeof(BlendBackwardSmem), s>>>(a);
 }
 
 }  // namespace tpd
