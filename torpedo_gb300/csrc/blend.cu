@@ -232,10 +232,11 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
                 const bool term = live && tn < kTMin;
                 const bool add = live && !term;
                 done = done || term;
-                const float w = __fmul_rn(alpha, T);
-                C0 = add ? __fmaf_rn(col.x, w, C0) : C0;
-                C1 = add ? __fmaf_rn(col.y, w, C1) : C1;
-                C2 = add ? __fmaf_rn(col.z, w, C2) : C2;
+                // a pair that does not contribute adds col * 0: C stays the same for finite colours
+                const float w = add ? __fmul_rn(alpha, T) : 0.0f;
+                C0 = __fmaf_rn(col.x, w, C0);
+                C1 = __fmaf_rn(col.y, w, C1);
+                C2 = __fmaf_rn(col.z, w, C2);
                 T = add ? tn : T;
                 last = add ? b0 + jj - start + 1 : last;
             }
