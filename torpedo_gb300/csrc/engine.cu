@@ -225,7 +225,12 @@ int wait_stream(tpd_engine* e) {
                                                (e->last_error.rfind("stage", 0) == 0 ? " (" + e->last_error + ")" : ""));
         const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (dt > limit) return fail(e, TPD_ERR_TIMEOUT, "frame did not finish within the host wait limit");
-        std::this_thread::sleep_for(std::chrono::microseconds(dt < 0.01 ? 20 : 500));
+        // frames take about a millisecond: poll without sleeping at first (a
+        // sleep of a few microseconds lasts tens on Linux), then back off
+        if (dt < 0.005)
+            std::this_thread::yield();
+        else
+            std::this_thread::sleep_for(std::chrono::microseconds(dt < 0.05 ? 50 : 500));
     }
 }
 
