@@ -162,6 +162,18 @@ TPD_API int tpd_raster_frame(tpd_engine* e, tpd_frame_stats* stats);
 TPD_API int tpd_raster_frames_async(tpd_engine* e, uint32_t count);
 TPD_API int tpd_sync(tpd_engine* e, tpd_frame_stats* stats);
 
+/* Pipelined rendering, no counterpart in the reference (its rasterFrame waits):
+ * tpd_render_async renders the current view(s) and copies the image (format
+ * TPD_IMAGE_*) to dst without waiting; the copy runs on a second stream beside
+ * the next frame. The camera constants and transforms are taken when the call
+ * is made, so tpd_set_camera may be called again at once. At most two renders
+ * may be outstanding; tpd_wait_render waits for the oldest, fills its stats and
+ * returns its status (TPD_ERR_CAPACITY: keys outgrew the buffers, render with
+ * tpd_raster_frame). dst must stay valid and unread until then. Needs a frame
+ * rendered with tpd_raster_frame after any change. */
+TPD_API int tpd_render_async(tpd_engine* e, void* dst, uint32_t format, int dst_is_device);
+TPD_API int tpd_wait_render(tpd_engine* e, tpd_frame_stats* stats);
+
 /* Accumulated per-stage GPU time (ms, TPD_STAGE_COUNT entries) and frame count
  * since the last reset, when the engine was created with stage_timing = 1. */
 TPD_API int tpd_stage_times(tpd_engine* e, double* ms, uint64_t* frames, int reset);

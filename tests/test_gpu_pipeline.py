@@ -171,3 +171,51 @@ def test_graph_replay_matches_eager(cuda):
     eng.close()
     assert first["keys"] == again["keys"]
     np.testing.assert_array_equal(img1, img2)
+
+
+def test_render_async_pipelined_matches_synchronous(cuda):
+    """tpd_render_async / tpd_wait_render with two renders in flight and the
+    camera changed between them give the synchronous frames bit for bit
+    (RGBA8 into pinned host memory, RGB32F into device memory); a third
+    outstanding render is refused."""
+    torch = cuda
+    recs, cam = _scene("cfg0")
+    cam2 = T.Camera.orbit((0.7, -0.4, -4.2), cam.width, cam.height)
+    ref = {}
+    for name, c in (("a", cam), ("b", cam2)):
+        e = T.GaussianEngine()
+        e.compile(recs)
+        e.set_camera(c)
+        e.raster_frame()
+        ref[name] = (e.read_image(rgba8=True)[0].copy(), e.read_image()[0].copy())
+        e.close()
+    eng = T.GaussianEngine()
+    eng.compile(recs)
+    eng.set_camera(cam)
+    eng.raster_frame()
+    px = cam.width * cam.height
+    host = [torch.zeros(px * 4, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    dev = [torch.zeros(px * 3, dtype=torch.float32, device="cuda") for _ in range(2)]
+    order = ["a", "b", "a", "b"]
+    for rgba in (True, False):
+        bufs = host if rgba else dev
+        for i, name in enumerate(order):
+            eng.set_camera(cam if name == "a" else cam2)
+            eng.render_async(bufs[i % 2], rgba8=rgba)
+            if i == 1:
+                with pytest.raises(T.TpdError):  # a third render while two are outstanding
+                    eng.render_async(bufs[0], rgba8=rgba)
+            if i >= 1:
+                st = eng.wait_render()
+                assert st["status"] == 0
+                prev = order[i - 1]
+                got = bufs[(i - 1) % 2].cpu().numpy()
+                if rgba:
+                    np.testing.assert_array_equal(got.reshape(cam.height, cam.width, 4), ref[prev][0])
+                else:
+                    np.testing.assert_array_equal(got.reshape(cam.height, cam.width, 3), ref[prev][1])
+        eng.wait_render()
+        got = bufs[(len(order) - 1) % 2].cpu().numpy()
+        last = ref[order[-1]][0 if rgba else 1]
+        np.testing.assert_array_equal(got.reshape(last.shape), last)
+    eng.close()

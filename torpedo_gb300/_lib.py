@@ -82,6 +82,8 @@ SIGNATURES = {
     "tpd_read_image": (C.c_int, [_P, _P, _U32, C.c_int]),
     "tpd_backward": (C.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "tpd_step_async": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _U32]),
+    "tpd_render_async": (C.c_int, [_P, _P, _U32, C.c_int]),
+    "tpd_wait_render": (C.c_int, [_P, _P]),
     "tpd_get_buffer": (C.c_int, [_P, _U32, C.POINTER(_P), C.POINTER(C.c_uint64)]),
     "tpd_read_buffer": (C.c_int, [_P, _U32, _P, C.c_uint64, C.c_uint64, C.c_int]),
     "tpd_get_stream": (_P, [_P]),

@@ -126,6 +126,24 @@ struct tpd_engine {
     // forward + backward step graph (tpd_step_async), keyed by the caller's pointers
     cudaGraphExec_t step_graph = nullptr;
     const void* step_key[6] = {};
+
+    // pipelined renders (tpd_render_async / tpd_wait_render): a ring of slots,
+    // each with its own pinned copy of the frame's constants and stats, a
+    // device staging image and completion events; the image copy to the
+    // caller runs on copy_stream, so the next frame computes meanwhile
+    static constexpr int kRing = 2;
+    cudaGraphExec_t body_graph = nullptr;  // the frame without uploads and stats copy
+    cudaStream_t copy_stream = nullptr;
+    ViewConst* ring_views[kRing] = {};
+    float* ring_transforms[kRing] = {};
+    uint32_t ring_transforms_cap = 0;
+    StatsHead* ring_stats[kRing] = {};
+    unsigned char* ring_image[kRing] = {};
+    uint64_t ring_image_cap = 0;
+    cudaEvent_t ring_ready[kRing] = {};  // main stream: frame, staging image and stats done
+    cudaEvent_t ring_done[kRing] = {};   // copy stream: the caller's image written
+    bool ring_busy[kRing] = {};
+    uint64_t ring_next = 0, ring_oldest = 0;
 };
 
 namespace {
@@ -164,6 +182,8 @@ void invalidate_graph(tpd_engine* e) {
     e->graph_valid = false;
     e->needs_eager = true;
     invalidate_step_graph(e);
+    if (e->body_graph) cudaGraphExecDestroy(e->body_graph);
+    e->body_graph = nullptr;
 }
 
 // Views x n sized buffers.
@@ -213,12 +233,19 @@ int ensure_key_capacity(tpd_engine* e, uint64_t want) {
     return TPD_OK;
 }
 
+int wait_event(tpd_engine* e, cudaEvent_t ev);
+
 int wait_stream(tpd_engine* e) {
     TPD_CUDA(e, cudaEventRecord(e->done_event, e->stream));
+    return wait_event(e, e->done_event);
+}
+
+// Polls ev with the engine's host wait limit.
+int wait_event(tpd_engine* e, cudaEvent_t ev) {
     const double limit = e->settings.timeout_s > 0 ? e->settings.timeout_s : 60.0;
     const auto t0 = std::chrono::steady_clock::now();
     while (true) {
-        const cudaError_t q = cudaEventQuery(e->done_event);
+        const cudaError_t q = cudaEventQuery(ev);
         if (q == cudaSuccess) return TPD_OK;
         if (q != cudaErrorNotReady)
             return fail(e, TPD_ERR_DEVICE, std::string("frame: ") + cudaGetErrorString(q) +
@@ -250,7 +277,9 @@ void harvest_all(tpd_engine* e) {
 }
 
 // Enqueues one frame on the stream (no host synchronisation).
-void enqueue_frame(tpd_engine* e) {
+// io = false leaves out the uploads of the view constants and transforms and
+// the stats copy (the pipelined renders enqueue those per slot).
+void enqueue_frame(tpd_engine* e, bool io = true) {
     cudaStream_t s = e->stream;
     cudaEvent_t* ev = nullptr;
     if (e->settings.stage_timing) {
@@ -280,9 +309,12 @@ void enqueue_frame(tpd_engine* e) {
         }
     };
     mark(0);
-    cudaMemcpyAsync(e->d_views, e->h_views, sizeof(ViewConst) * e->n_views, cudaMemcpyHostToDevice, s);
-    if (!e->identity_transforms)
-        cudaMemcpyAsync(e->d_transforms, e->h_transforms, sizeof(float) * 16 * e->n_ent, cudaMemcpyHostToDevice, s);
+    if (io) {
+        cudaMemcpyAsync(e->d_views, e->h_views, sizeof(ViewConst) * e->n_views, cudaMemcpyHostToDevice, s);
+        if (!e->identity_transforms)
+            cudaMemcpyAsync(e->d_transforms, e->h_transforms, sizeof(float) * 16 * e->n_ent, cudaMemcpyHostToDevice,
+                            s);
+    }
     launch_frame_begin(e->d_ctl, e->identity_transforms ? nullptr : e->d_transforms, e->n_ent, e->d_views,
                        e->n_views, e->d_ent_mats, s);
     PreprocessArgs pa{};
@@ -357,7 +389,7 @@ void enqueue_frame(tpd_engine* e) {
     ba.n_contrib = e->d_n_contrib;
     launch_blend(ba, s);
     mark(6);
-    cudaMemcpyAsync(e->h_stats, e->d_ctl, sizeof(StatsHead), cudaMemcpyDeviceToHost, s);
+    if (io) cudaMemcpyAsync(e->h_stats, e->d_ctl, sizeof(StatsHead), cudaMemcpyDeviceToHost, s);
 }
 
 int run_frame_once(tpd_engine* e, bool use_graph) {
@@ -465,18 +497,67 @@ int alloc_scene(tpd_engine* e, uint32_t n, uint32_t n_ent) {
     return TPD_OK;
 }
 
-void fill_stats(tpd_engine* e, tpd_frame_stats* stats, uint32_t retries) {
+void fill_stats_from(tpd_engine* e, const StatsHead& h, tpd_frame_stats* stats, uint32_t retries) {
     if (!stats) return;
     std::memset(stats, 0, sizeof(*stats));
-    stats->keys = e->h_stats->total_keys;
+    stats->keys = h.total_keys;
     stats->key_capacity = e->capacity;
-    stats->visible = e->h_stats->visible;
+    stats->visible = h.visible;
     stats->tiles = e->total_tiles;
     stats->key_bits = e->key_bits;
     stats->sort_passes = e->passes;
-    stats->status = e->h_stats->status;
+    stats->status = h.status;
     stats->retries = retries;
     stats->views = e->n_views;
+}
+
+void fill_stats(tpd_engine* e, tpd_frame_stats* stats, uint32_t retries) {
+    fill_stats_from(e, *e->h_stats, stats, retries);
+}
+
+// Pinned ring slots and staging images of the pipelined renders, sized for
+// the current views and transforms (before any render is outstanding).
+int ensure_ring(tpd_engine* e) {
+    if (!e->copy_stream) {
+        TPD_CUDA(e, cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < tpd_engine::kRing; ++i) {
+            TPD_CUDA(e, cudaMallocHost(reinterpret_cast<void**>(&e->ring_views[i]), sizeof(ViewConst) * kMaxViews));
+            TPD_CUDA(e, cudaMallocHost(reinterpret_cast<void**>(&e->ring_stats[i]), sizeof(StatsHead)));
+            TPD_CUDA(e, cudaEventCreateWithFlags(&e->ring_ready[i], cudaEventDisableTiming));
+            TPD_CUDA(e, cudaEventCreateWithFlags(&e->ring_done[i], cudaEventDisableTiming));
+        }
+    }
+    if (!e->identity_transforms && e->n_ent > e->ring_transforms_cap) {
+        for (int i = 0; i < tpd_engine::kRing; ++i) {
+            if (e->ring_transforms[i]) cudaFreeHost(e->ring_transforms[i]);
+            e->ring_transforms[i] = nullptr;
+            TPD_CUDA(e, cudaMallocHost(reinterpret_cast<void**>(&e->ring_transforms[i]), sizeof(float) * 16 * e->n_ent));
+        }
+        e->ring_transforms_cap = e->n_ent;
+    }
+    const uint64_t bytes = e->total_pixels * 12;  // room for RGB32F
+    if (bytes > e->ring_image_cap) {
+        for (int i = 0; i < tpd_engine::kRing; ++i) TPD_CUDA(e, dalloc(e->ring_image[i], bytes));
+        e->ring_image_cap = bytes;
+    }
+    return TPD_OK;
+}
+
+// Status of a finished frame, as tpd_raster_frame reports it.
+int frame_status(tpd_engine* e, const StatsHead& h) {
+    if (h.status & kStatusKeyOverflow) {
+        e->frame_valid = false;
+        return fail(e, TPD_ERR_CAPACITY, "keys outgrew the key buffers; render with tpd_raster_frame");
+    }
+    if (h.status & kStatusBadIndex) {
+        uint32_t dbg[4] = {0, 0, 0, 0};
+        cudaMemcpy(dbg, e->d_ctl->debug, sizeof(dbg), cudaMemcpyDeviceToHost);
+        return fail(e, TPD_ERR_DEVICE, "bounds check failed: site " + std::to_string(dbg[0]) + " index " +
+                                           std::to_string((uint64_t(dbg[3]) << 32) | dbg[1]) + " bound " +
+                                           std::to_string(dbg[2]));
+    }
+    if (h.status & kStatusFatal) return fail(e, TPD_ERR_TIMEOUT, "a bounded device wait ran out");
+    return TPD_OK;
 }
 
 }  // namespace
@@ -580,6 +661,16 @@ void tpd_destroy(tpd_engine* e) {
     if (e->h_stats) cudaFreeHost(e->h_stats);
     if (e->h_views) cudaFreeHost(e->h_views);
     if (e->h_transforms) cudaFreeHost(e->h_transforms);
+    if (e->copy_stream) cudaStreamSynchronize(e->copy_stream);
+    for (int i = 0; i < tpd_engine::kRing; ++i) {
+        if (e->ring_views[i]) cudaFreeHost(e->ring_views[i]);
+        if (e->ring_transforms[i]) cudaFreeHost(e->ring_transforms[i]);
+        if (e->ring_stats[i]) cudaFreeHost(e->ring_stats[i]);
+        dfree(e->ring_image[i]);
+        if (e->ring_ready[i]) cudaEventDestroy(e->ring_ready[i]);
+        if (e->ring_done[i]) cudaEventDestroy(e->ring_done[i]);
+    }
+    if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
     if (e->done_event) cudaEventDestroy(e->done_event);
     for (int i = 0; i < tpd_engine::kTimingSlots; ++i)
         for (int k = 0; k < tpd_engine::kTimingEvents; ++k)
@@ -743,6 +834,85 @@ int tpd_sync(tpd_engine* e, tpd_frame_stats* stats) {
     }
     if (h.status & kStatusFatal) return fail(e, TPD_ERR_TIMEOUT, "a bounded device wait ran out");
     return TPD_OK;
+}
+
+int tpd_render_async(tpd_engine* e, void* dst, uint32_t format, int dst_is_device) {
+    if (!e || !dst) return TPD_ERR_ARG;
+    if (format != TPD_IMAGE_RGB32F && format != TPD_IMAGE_RGBA8) return fail(e, TPD_ERR_ARG, "unknown image format");
+    if (!e->frame_valid || e->needs_eager)
+        return fail(e, TPD_ERR_STATE, "render one frame with tpd_raster_frame after any change first");
+    cudaSetDevice(e->device);
+    const int slot = int(e->ring_next % tpd_engine::kRing);
+    if (e->ring_busy[slot]) return fail(e, TPD_ERR_STATE, "two renders outstanding: call tpd_wait_render first");
+    if (e->ring_oldest == e->ring_next) {  // nothing outstanding: buffers may be resized
+        const int rc = ensure_ring(e);
+        if (rc != TPD_OK) return rc;
+    } else if (e->total_pixels * 12 > e->ring_image_cap ||
+               (!e->identity_transforms && e->n_ent > e->ring_transforms_cap)) {
+        return fail(e, TPD_ERR_STATE, "the views grew while renders are outstanding: call tpd_wait_render first");
+    }
+    cudaStream_t s = e->stream;
+    // the frame's constants, snapshotted into the slot (its last render has been waited for)
+    std::memcpy(e->ring_views[slot], e->h_views, sizeof(ViewConst) * e->n_views);
+    TPD_CUDA(e, cudaMemcpyAsync(e->d_views, e->ring_views[slot], sizeof(ViewConst) * e->n_views,
+                                cudaMemcpyHostToDevice, s));
+    if (!e->identity_transforms) {
+        std::memcpy(e->ring_transforms[slot], e->h_transforms, sizeof(float) * 16 * e->n_ent);
+        TPD_CUDA(e, cudaMemcpyAsync(e->d_transforms, e->ring_transforms[slot], sizeof(float) * 16 * e->n_ent,
+                                    cudaMemcpyHostToDevice, s));
+    }
+    const bool graph = e->settings.use_graph && !e->settings.stage_timing;
+    if (graph) {
+        if (!e->body_graph) {
+            cudaGraph_t g = nullptr;
+            TPD_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            enqueue_frame(e, false);
+            TPD_CUDA(e, cudaStreamEndCapture(s, &g));
+            cudaGraphExec_t ge = nullptr;
+            const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            TPD_CUDA(e, err);
+            e->body_graph = ge;
+        }
+        TPD_CUDA(e, cudaGraphLaunch(e->body_graph, s));
+    } else {
+        enqueue_frame(e, false);
+    }
+    // image into the slot's staging buffer and stats into its pinned slot
+    uint64_t bytes;
+    if (format == TPD_IMAGE_RGBA8) {
+        launch_pack_rgba8(e->d_image, reinterpret_cast<uint32_t*>(e->ring_image[slot]), e->total_pixels, s);
+        bytes = e->total_pixels * 4;
+    } else {
+        TPD_CUDA(e, cudaMemcpyAsync(e->ring_image[slot], e->d_image, e->total_pixels * 12, cudaMemcpyDeviceToDevice, s));
+        bytes = e->total_pixels * 12;
+    }
+    TPD_CUDA(e, cudaMemcpyAsync(e->ring_stats[slot], e->d_ctl, sizeof(StatsHead), cudaMemcpyDeviceToHost, s));
+    TPD_CUDA(e, cudaEventRecord(e->ring_ready[slot], s));
+    // the caller's copy runs beside the next frame
+    TPD_CUDA(e, cudaStreamWaitEvent(e->copy_stream, e->ring_ready[slot], 0));
+    TPD_CUDA(e, cudaMemcpyAsync(dst, e->ring_image[slot], bytes,
+                                dst_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, e->copy_stream));
+    TPD_CUDA(e, cudaEventRecord(e->ring_done[slot], e->copy_stream));
+    TPD_CUDA(e, cudaGetLastError());
+    e->ring_busy[slot] = true;
+    ++e->ring_next;
+    ++e->frames;
+    return TPD_OK;
+}
+
+int tpd_wait_render(tpd_engine* e, tpd_frame_stats* stats) {
+    if (!e) return TPD_ERR_ARG;
+    if (e->ring_oldest == e->ring_next) return fail(e, TPD_ERR_STATE, "no render outstanding");
+    cudaSetDevice(e->device);
+    const int slot = int(e->ring_oldest % tpd_engine::kRing);
+    const int rc = wait_event(e, e->ring_done[slot]);
+    if (rc != TPD_OK) return rc;
+    e->ring_busy[slot] = false;
+    ++e->ring_oldest;
+    const StatsHead h = *e->ring_stats[slot];
+    fill_stats_from(e, h, stats, 0);
+    return frame_status(e, h);
 }
 
 int tpd_stage_times(tpd_engine* e, double* ms, uint64_t* frames, int reset) {

@@ -313,6 +313,20 @@ class GaussianEngine:
                                      g_quats.data_ptr(), g_logits.data_ptr(), g_sh.data_ptr()), self._h)
         return g_means, g_log_scales, g_quats, g_logits, g_sh
 
+    def render_async(self, dst, rgba8: bool = True) -> None:
+        """Renders the current view(s) and copies the image into dst (a pinned
+        host or CUDA tensor of pixels * 4 bytes for RGBA8, pixels * 3 floats
+        otherwise) without waiting; wait_render() waits for the oldest of at
+        most two outstanding renders and returns its stats."""
+        fmt = L.TPD_IMAGE_RGBA8 if rgba8 else L.TPD_IMAGE_RGB32F
+        on_device = 1 if getattr(dst, "is_cuda", False) else 0
+        _check(L.load().tpd_render_async(self._h, dst.data_ptr(), fmt, on_device), self._h)
+
+    def wait_render(self) -> dict:
+        st = L.FrameStats()
+        _check(L.load().tpd_wait_render(self._h, C.byref(st)), self._h)
+        return st.as_dict()
+
     def step_async(self, dL_dimage, grads, count: int = 1):
         """count training steps (forward frame + backward) enqueued on the engine's
         stream without host waits; grads = (g_means, g_log_scales, g_quats,
