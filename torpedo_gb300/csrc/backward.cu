@@ -50,15 +50,30 @@ __device__ __forceinline__ void sh_basis(int k, float x, float y, float z, float
     }
 }
 
-__global__ void __launch_bounds__(128) preprocess_backward_kernel(PreprocessBackwardArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const float* rec = a.recs + size_t(i) * kRecordFloats;
+constexpr uint32_t kBwdThreads = 128;
+
+// A block's records are staged into shared memory with coalesced 16-byte
+// loads (a record is 240 B, so thread-per-record loads would stride), and its
+// SH gradients leave through the same buffer as coalesced 16-byte stores.
+__global__ void __launch_bounds__(kBwdThreads) preprocess_backward_kernel(PreprocessBackwardArgs a) {
+    __shared__ __align__(16) float srec[kBwdThreads * kRecordFloats];  // 30 KB; reused for the SH gradients
+    const uint32_t base = blockIdx.x * kBwdThreads;
+    const uint32_t cnt = min(kBwdThreads, a.n - base);
+    {
+        const float4* src = reinterpret_cast<const float4*>(a.recs + size_t(base) * kRecordFloats);
+        float4* dst = reinterpret_cast<float4*>(srec);
+        for (uint32_t k = threadIdx.x; k < cnt * (kRecordFloats / 4); k += kBwdThreads) dst[k] = src[k];
+    }
+    __syncthreads();
+    const uint32_t i = base + threadIdx.x;
+    const bool active = threadIdx.x < cnt;
+    const float* rec = srec + threadIdx.x * kRecordFloats;
+    if (!active) rec = srec;  // any staged record: results of inactive threads are not stored
     const float m[3] = {rec[0], rec[1], rec[2]};
     const float op = rec[3];
     const float qx = rec[4], qy = rec[5], qz = rec[6], qw = rec[7];
     const float s[3] = {rec[8] * rec[11], rec[9] * rec[11], rec[10] * rec[11]};
-    const uint32_t e = a.ent_idx ? a.ent_idx[i] : 0u;
+    const uint32_t e = (a.ent_idx && active) ? a.ent_idx[i] : 0u;
     const int nf = a.sh_degree >= 3 ? 15 : a.sh_degree == 2 ? 8 : a.sh_degree == 1 ? 3 : 0;
     const bool compat = a.band3_compat != 0;
 
@@ -84,10 +99,14 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(PreprocessBack
 #pragma unroll
     for (int k = 0; k < 48; ++k) gsh[k] = 0.f;
 
-    for (uint32_t v = 0; v < a.n_views; ++v) {
-        const Splat& sp = a.splats[size_t(v) * a.n + i];
-        if (!(sp.radius > 0.0f)) continue;
-        const float* g = a.g2d + (size_t(v) * a.n + i) * kG2DStride;
+    for (uint32_t v = 0; v < a.n_views && active; ++v) {
+        // the splat (colour, tiles | texel | conic, opacity) and its gradient record, 16 bytes at a time
+        const float4* sp4 = reinterpret_cast<const float4*>(a.splats + size_t(v) * a.n + i);
+        const float4 sp_c = sp4[0], sp_t = sp4[1];
+        if (!(sp_t.w > 0.0f)) continue;
+        const float4* g4 = reinterpret_cast<const float4*>(a.g2d + (size_t(v) * a.n + i) * kG2DStride);
+        const float4 ga4 = g4[0], gb4 = g4[1], gc4 = g4[2];
+        const float g[9] = {ga4.x, ga4.y, ga4.z, ga4.w, gb4.x, gb4.y, gb4.z, gb4.w, gc4.x};
         const ViewConst& vc = a.views[v];
         const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
         float vp[3], cp[4];
@@ -110,14 +129,16 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(PreprocessBack
         const float d0 = m[0] - campos[0], d1 = m[1] - campos[1], d2 = m[2] - campos[2];
         const float vlen = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
         const float x = d0 / vlen, y = d1 / vlen, z = d2 / vlen;
-        const float col[3] = {sp.r, sp.g, sp.b};
+        const float col[3] = {sp_c.x, sp_c.y, sp_c.z};
         float graw[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) graw[c] = col[c] > 0.f ? g[6 + c] : 0.f;
         float gd0 = 0.f, gd1 = 0.f, gd2 = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) gsh[c] += graw[c] * SH_C0;
-        for (int k = 1; k <= nf; ++k) {
+#pragma unroll
+        for (int k = 1; k <= 15; ++k) {
+            if (k > nf) break;
             float b, b0, b1, b2;
             sh_basis(k, x, y, z, b, b0, b1, b2);
 #pragma unroll
@@ -217,10 +238,9 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(PreprocessBack
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int c = 0; c < 3; ++c) gR[r * 3 + c] = gM[r * 3 + c] * s[c];
-    float* gls = a.g_log_scales + size_t(i) * 3;
+    float gq[4], glsv[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) gls[c] = (gM[0 * 3 + c] * R[0 * 3 + c] + gM[1 * 3 + c] * R[1 * 3 + c] + gM[2 * 3 + c] * R[2 * 3 + c]) * s[c];
-    float* gq = a.g_quats + size_t(i) * 4;
+    for (int c = 0; c < 3; ++c) glsv[c] = (gM[0 * 3 + c] * R[0 * 3 + c] + gM[1 * 3 + c] * R[1 * 3 + c] + gM[2 * 3 + c] * R[2 * 3 + c]) * s[c];
     gq[0] = gR[1] * 2.f * qy + gR[2] * 2.f * qz + gR[3] * 2.f * qy + gR[4] * (-4.f * qx) + gR[5] * (-2.f * qw) +
             gR[6] * 2.f * qz + gR[7] * 2.f * qw + gR[8] * (-4.f * qx);
     gq[1] = gR[0] * (-4.f * qy) + gR[1] * 2.f * qx + gR[2] * 2.f * qw + gR[3] * 2.f * qx + gR[5] * 2.f * qz +
@@ -229,21 +249,48 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(PreprocessBack
             gR[5] * 2.f * qy + gR[6] * 2.f * qx + gR[7] * 2.f * qy;
     gq[3] = gR[1] * (-2.f * qz) + gR[2] * 2.f * qy + gR[3] * 2.f * qz + gR[5] * (-2.f * qx) + gR[6] * (-2.f * qy) +
             gR[7] * 2.f * qx;
-    float* gmo = a.g_means + size_t(i) * 3;
-    gmo[0] = gm[0];
-    gmo[1] = gm[1];
-    gmo[2] = gm[2];
-    a.g_logits[i] = glogit;
-    float* gs = a.g_sh + size_t(i) * 48;
+    if (active) {
+        float* gls = a.g_log_scales + size_t(i) * 3;
+        gls[0] = glsv[0];
+        gls[1] = glsv[1];
+        gls[2] = glsv[2];
+        if ((reinterpret_cast<uintptr_t>(a.g_quats) & 15u) == 0) {
+            reinterpret_cast<float4*>(a.g_quats)[i] = make_float4(gq[0], gq[1], gq[2], gq[3]);
+        } else {
+            float* gqo = a.g_quats + size_t(i) * 4;
+            gqo[0] = gq[0];
+            gqo[1] = gq[1];
+            gqo[2] = gq[2];
+            gqo[3] = gq[3];
+        }
+    }
+    __syncthreads();  // every thread is done with the staged records
+    if (active) {
+        float* gmo = a.g_means + size_t(i) * 3;
+        gmo[0] = gm[0];
+        gmo[1] = gm[1];
+        gmo[2] = gm[2];
+        a.g_logits[i] = glogit;
+        float4* mine = reinterpret_cast<float4*>(srec + threadIdx.x * 48);
 #pragma unroll
-    for (int k = 0; k < 48; ++k) gs[k] = gsh[k];
+        for (int k = 0; k < 12; ++k) mine[k] = make_float4(gsh[4 * k], gsh[4 * k + 1], gsh[4 * k + 2], gsh[4 * k + 3]);
+    }
+    __syncthreads();
+    if ((reinterpret_cast<uintptr_t>(a.g_sh) & 15u) == 0) {
+        float4* gs = reinterpret_cast<float4*>(a.g_sh + size_t(base) * 48);
+        const float4* from = reinterpret_cast<const float4*>(srec);
+        for (uint32_t k = threadIdx.x; k < cnt * 12; k += kBwdThreads) gs[k] = from[k];
+    } else {  // a caller's buffer that is not 16-byte aligned
+        float* gs = a.g_sh + size_t(base) * 48;
+        for (uint32_t k = threadIdx.x; k < cnt * 48; k += kBwdThreads) gs[k] = srec[k];
+    }
 }
 
 }  // namespace
 
 void launch_preprocess_backward(const PreprocessBackwardArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
-    preprocess_backward_kernel<<<(a.n + 127) / 128, 128, 0, s>>>(a);
+    preprocess_backward_kernel<<<(a.n + kBwdThreads - 1) / kBwdThreads, kBwdThreads, 0, s>>>(a);
 }
 
 }  // namespace tpd

@@ -968,13 +968,14 @@ int prepare_backward(tpd_engine* e, BackwardOut& o) {
         TPD_CUDA(e, dalloc(e->d_gscratch, gs));
         e->gscratch_cap = gs;
     }
+    // scratch sections: quaternions and SH first, so both start 16-byte aligned
     float* sc = e->d_gscratch;
     const uint64_t n = e->n;
-    if (!o.means) o.means = sc;
-    if (!o.log_scales) o.log_scales = sc + n * 3;
-    if (!o.quats) o.quats = sc + n * 6;
-    if (!o.logits) o.logits = sc + n * 10;
-    if (!o.sh) o.sh = sc + n * 11;
+    if (!o.quats) o.quats = sc;
+    if (!o.sh) o.sh = sc + n * 4;
+    if (!o.means) o.means = sc + n * 52;
+    if (!o.log_scales) o.log_scales = sc + n * 55;
+    if (!o.logits) o.logits = sc + n * 58;
     return TPD_OK;
 }
 
