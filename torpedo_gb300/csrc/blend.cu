@@ -405,28 +405,30 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
                 const float G = ex2_approx(p2);
                 const float raw = __fmul_rn(col.w, G);
                 const float alpha = fminf(kAlphaMax, raw);
-                const float inv = __frcp_rn(1.0f - alpha);
+                const float inv = __fdividef(1.0f, 1.0f - alpha);  // 1 - alpha >= 0.01
                 const float Tb = T * inv;  // transmittance in front of this entry
-                const float w = alpha * Tb;
+                // zero weight and gradient scale for pairs that do not count:
+                // every term below is finite, so it adds exactly nothing
+                const float w = contrib ? alpha * Tb : 0.0f;
                 const float dA = g0 * (col.x * Tb - S0 * inv) + g1 * (col.y * Tb - S1 * inv) +
                                  g2 * (col.z * Tb - S2 * inv);
-                S0 = contrib ? fmaf(col.x, w, S0) : S0;
-                S1 = contrib ? fmaf(col.y, w, S1) : S1;
-                S2 = contrib ? fmaf(col.z, w, S2) : S2;
+                S0 = fmaf(col.x, w, S0);
+                S1 = fmaf(col.y, w, S1);
+                S2 = fmaf(col.z, w, S2);
                 T = contrib ? Tb : T;
                 // power = p2 ln2; d power / d(dx, dy) = ln2 (2 qa dx + qb dy, 2 qc dy + qb dx)
                 const bool unclamped = contrib && raw <= kAlphaMax;
-                const float dpow = dA * alpha;
+                const float dpow = unclamped ? dA * alpha : 0.0f;
                 float gv[kG2D];
-                gv[0] = unclamped ? dpow * kLn2 * (2.0f * q.x * dx + q.y * dy) : 0.0f;
-                gv[1] = unclamped ? dpow * kLn2 * (2.0f * q.z * dy + q.y * dx) : 0.0f;
-                gv[2] = unclamped ? dpow * (-0.5f * dx * dx) : 0.0f;
-                gv[3] = unclamped ? dpow * (-dx * dy) : 0.0f;
-                gv[4] = unclamped ? dpow * (-0.5f * dy * dy) : 0.0f;
+                gv[0] = dpow * kLn2 * (2.0f * q.x * dx + q.y * dy);
+                gv[1] = dpow * kLn2 * (2.0f * q.z * dy + q.y * dx);
+                gv[2] = dpow * (-0.5f * dx * dx);
+                gv[3] = dpow * (-dx * dy);
+                gv[4] = dpow * (-0.5f * dy * dy);
                 gv[5] = unclamped ? dA * G : 0.0f;
-                gv[6] = contrib ? g0 * w : 0.0f;
-                gv[7] = contrib ? g1 * w : 0.0f;
-                gv[8] = contrib ? g2 * w : 0.0f;
+                gv[6] = g0 * w;
+                gv[7] = g1 * w;
+                gv[8] = g2 * w;
                 if (__any_sync(0xFFFFFFFFu, contrib)) {
                     const float lo[8] = {gv[0], gv[1], gv[2], gv[3], gv[4], gv[5], gv[6], gv[7]};
                     const float rs = warp_sum8_transposed(lo, lane);
