@@ -90,3 +90,25 @@ def sh_probe(k: int):
     sh[3 + 0 * 15 + (k - 1)] = 1.0
     rec = record((0.3, -0.2, 0.5), 0.9, (0.05,) * 3, sh=sh)[None]
     return rec, cam
+
+
+def screen_filling():
+    """One large opaque Gaussian just in front of the camera that covers every
+    tile of a 160x96 image, with a few small ones behind and in front of it:
+    one Gaussian contributes a key to all 60 tiles."""
+    cam = camera(160, 96)
+    recs = [record((0.0, 0.0, -3.0), 0.9, (0.6, 0.5, 0.4), quat=(0.2, 0.1, 0.0, 0.97), sh=rgb2sh(0.3, 0.6, 0.2))]
+    rng = np.random.default_rng(11)
+    for _ in range(40):
+        z = float(rng.uniform(-3.8, 1.0))
+        recs.append(record((float(rng.uniform(-1, 1)), float(rng.uniform(-0.6, 0.6)), z), float(rng.uniform(0.2, 0.9)),
+                           tuple(float(v) for v in rng.uniform(0.01, 0.08, 3)),
+                           sh=rgb2sh(*(float(c) for c in rng.uniform(0, 1, 3)))))
+    return np.stack(recs), cam
+
+
+def tiny_view():
+    """The cfg0-style random scene seen through a 5x3 image: one partial tile."""
+    recs = np.stack([record((float(x), float(y), float(z)), 0.7, (0.04, 0.05, 0.03), sh=rgb2sh(0.9, 0.5, 0.1))
+                     for x, y, z in np.random.default_rng(12).normal(0, 0.2, (300, 3))])
+    return recs, camera(5, 3)

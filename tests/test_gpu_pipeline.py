@@ -38,10 +38,15 @@ def _scene(name):
         return kat.tile_edge()
     if name == "kat_culled":
         return kat.culled()
+    if name == "kat_screen_filling":
+        return kat.screen_filling()
+    if name == "kat_tiny_view":
+        return kat.tiny_view()
     raise KeyError(name)
 
 
-SCENES = ["cfg0", "cfg1_200k", "cfg2_50k", "odd_size", "kat_single", "kat_two", "kat_edge", "kat_culled"]
+SCENES = ["cfg0", "cfg1_200k", "cfg2_50k", "odd_size", "kat_single", "kat_two", "kat_edge", "kat_culled",
+          "kat_screen_filling", "kat_tiny_view"]
 _cache = {}
 
 

@@ -322,27 +322,46 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
 // Exclusive scan of tile counts over partitions of 256 threads x 4 items
 // (prefix.slang:40-158); kGather: counts of splats[items[r]] (depth order),
 // else of splats[r]. Total -> ctl->total_keys, non-empty count -> ctl->visible.
-constexpr uint32_t kScanThreads = 256, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
+constexpr uint32_t kScanThreads = 256;
 
-template <bool kGather>
+// kItems consecutive items per thread: 4 for the standalone scan, 16 for the
+// depth-order scan of the frame (4096-item partitions: a quarter of the
+// look-back chain; the item indices are read 16 bytes at a time).
+template <bool kGather, uint32_t kItems>
 __global__ void __launch_bounds__(kScanThreads)
     scan_tiles_kernel(const Splat* splats, const uint32_t* items, uint32_t n, uint32_t* offsets, uint64_t* desc,
                       FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish) {
+    constexpr uint32_t kScanTile = kScanThreads * kItems;
     __shared__ uint32_t s_part, s_excl;
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if (tid == 0) s_part = atomicAdd(&ctl->ticket[kTicketScan], 1u);
     __syncthreads();
     const uint32_t part = s_part;
-    const uint32_t base = part * kScanTile + tid * kScanItems;
-    uint32_t v[kScanItems], sum = 0, vis = 0;
+    const uint32_t base = part * kScanTile + tid * kItems;
+    uint32_t it[kItems];
+    if constexpr (kGather && kItems % 4 == 0) {
 #pragma unroll
-    for (uint32_t k = 0; k < kScanItems; ++k) {
-        v[k] = 0;
-        if (base + k < n) {
-            const uint32_t it = kGather ? items[base + k] : base + k;
-            v[k] = splats[it].tiles;
+        for (uint32_t k = 0; k < kItems; k += 4) {
+            if (base + k + 3 < n) {
+                const uint4 q = *reinterpret_cast<const uint4*>(items + base + k);
+                it[k] = q.x;
+                it[k + 1] = q.y;
+                it[k + 2] = q.z;
+                it[k + 3] = q.w;
+            } else {
+#pragma unroll
+                for (uint32_t j = 0; j < 4; ++j) it[k + j] = base + k + j < n ? items[base + k + j] : 0u;
+            }
         }
+    } else {
+#pragma unroll
+        for (uint32_t k = 0; k < kItems; ++k) it[k] = kGather ? (base + k < n ? items[base + k] : 0u) : base + k;
+    }
+    uint32_t v[kItems], sum = 0, vis = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kItems; ++k) {
+        v[k] = base + k < n ? splats[it[k]].tiles : 0u;
         sum += v[k];
         vis += v[k] ? 1u : 0u;
     }
@@ -370,7 +389,7 @@ __global__ void __launch_bounds__(kScanThreads)
     __syncthreads();
     uint32_t run = s_excl + wbase + incl - sum;
 #pragma unroll
-    for (uint32_t k = 0; k < kScanItems; ++k) {
+    for (uint32_t k = 0; k < kItems; ++k) {
         if (base + k < n) offsets[base + k] = run;
         run += v[k];
     }
@@ -417,17 +436,17 @@ void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s) {
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
                        uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
     if (n == 0) return;
-    const uint32_t blocks = (n + kScanTile - 1) / kScanTile;
-    scan_tiles_kernel<false><<<blocks, kScanThreads, 0, s>>>(splats, nullptr, n, offsets, desc, ctl, spin_limit,
-                                                             never_publish);
+    const uint32_t blocks = (n + kScanThreads * 4 - 1) / (kScanThreads * 4);
+    scan_tiles_kernel<false, 4><<<blocks, kScanThreads, 0, s>>>(splats, nullptr, n, offsets, desc, ctl, spin_limit,
+                                                                never_publish);
 }
 
 void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t count, uint32_t* offsets, uint64_t* desc,
                        FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
     if (count == 0) return;
-    const uint32_t blocks = (count + kScanTile - 1) / kScanTile;
-    scan_tiles_kernel<true><<<blocks, kScanThreads, 0, s>>>(splats, items, count, offsets, desc, ctl, spin_limit,
-                                                            never_publish);
+    const uint32_t blocks = (count + kScanThreads * 16 - 1) / (kScanThreads * 16);
+    scan_tiles_kernel<true, 16><<<blocks, kScanThreads, 0, s>>>(splats, items, count, offsets, desc, ctl, spin_limit,
+                                                                never_publish);
 }
 
 void launch_pack_records(const float* means, const float* log_scales, const float* quats, const float* logits,
