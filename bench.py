@@ -446,6 +446,7 @@ def run_ours(args):
     passes = int(st["sort_passes"])  # tile-id passes of the key sort
     key_bits = int(st["key_bits"])
     hbm, peak_kind = peaks()
+    sort_formula = K * (8 + 24 * math.ceil(key_bits / 8))
     pass_ms = stage_avg["key_sort"] / passes
     achieved = K * 24 / (pass_ms / 1000.0) / 1e9
     traffic = None
@@ -503,7 +504,12 @@ def run_ours(args):
                      "bytes_per_launch": K * 24, "avg_launch_ms": round(pass_ms, 5)},
         "frame_sort": {"keys": K, "key_bits": key_bits, "tile_passes": passes,
                        "depth_sort_ms": round(stage_avg["depth_sort"], 4), "key_sort_ms": round(stage_avg["key_sort"], 4),
-                       "note": "Gaussians sorted by depth first (N items), then the K keys on their tile-id bits only"},
+                       "formula_GBps": round(sort_formula / ((stage_avg["depth_sort"] + stage_avg["key_sort"]) / 1000) / 1e9, 1),
+                       "frac_of_hbm": round(sort_formula / ((stage_avg["depth_sort"] + stage_avg["key_sort"]) / 1000) / 1e9
+                                            / hbm, 4),
+                       "note": "Gaussians sorted by depth first (N items, the depth-order tile-count scan included), "
+                               "then the K keys on their tile-id bits only; GB/s by the fixed formula "
+                               "K * (8 + 24 * ceil(B / 8)) bytes over that time"},
         "general_sort": general,
         "blend": blend,
         "stages_ms": {k: round(v, 4) for k, v in stage_avg.items()},

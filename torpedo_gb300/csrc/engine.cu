@@ -1141,6 +1141,7 @@ int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t*
     plan.key_bits = key_bits;
     plan.hist = ctl->sort_hist;
     plan.hist_ready = false;
+    plan.threads = 512;  // 512 threads x 8 keys per 4096-key partition: the faster variant on GB300
     const bool alt = launch_sort(keys, vals, keys_alt, vals_alt, n, plan, desc, ctl, kDefaultSpin, sms, s);
     *result_in_alt = alt ? 1 : 0;
     return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;
