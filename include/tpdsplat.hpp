@@ -136,6 +136,21 @@ public:
         return st;
     }
 
+    /* Pipelined rendering: renders `camera` and copies the RGBA8 image into
+     * dst (pinned host memory, width * height * 4 bytes) without waiting; at
+     * most two renders may be outstanding. waitRender() waits for the oldest
+     * and returns its stats; dst must stay untouched until then. */
+    void renderAsync(const Camera& camera, uint8_t* dst) {
+        check(tpd_set_camera(e_, camera.view, camera.projection, camera.width, camera.height), e_, "tpd_set_camera");
+        check(tpd_render_async(e_, dst, TPD_IMAGE_RGBA8, 0), e_, "tpd_render_async");
+    }
+
+    tpd_frame_stats waitRender() {
+        tpd_frame_stats st{};
+        check(tpd_wait_render(e_, &st), e_, "tpd_wait_render");
+        return st;
+    }
+
     /* The draw() step without a swapchain: the last frame as RGBA8 (alpha 255). */
     std::vector<uint8_t> readImageRGBA8() const {
         std::vector<uint8_t> out(size_t(width_) * height_ * 4);

@@ -23,6 +23,15 @@ int main(int argc, char** argv) {
         engine.getTransformHost()->transform(0, identity);
         const tpd_frame_stats st = engine.rasterFrame(camera);
         const std::vector<float> rgb = engine.readImageRGB();
+        // the same frame through the pipelined calls must give the same RGBA8 image
+        const std::vector<uint8_t> rgba = engine.readImageRGBA8();
+        std::vector<uint8_t> piped(rgba.size());
+        engine.renderAsync(camera, piped.data());
+        engine.waitRender();
+        if (piped != rgba) {
+            std::fprintf(stderr, "pipelined frame differs\n");
+            return 4;
+        }
         FILE* f = std::fopen(argv[1], "wb");
         if (!f || std::fwrite(rgb.data(), sizeof(float), rgb.size(), f) != rgb.size()) return 3;
         std::fclose(f);

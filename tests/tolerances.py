@@ -1,7 +1,7 @@
 """Tolerances of the parity tests, stated once.
 
 Preprocess (Splat fields) must agree to relative error 1e-5, where "relative"
-divides by a per-field scale so that values near zero are judged against the
+divides by a per-field scale so that values near zero are compared against the
 quantity they belong to:
   colour r, g, b      max(|ref|, 1)
   px, py              max(|ref|, image width / height)
