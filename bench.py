@@ -331,7 +331,7 @@ def run_train_only(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream(torch.device("cuda", 0))
     settings = {"sort_ctas_per_sm": args.sort_ctas or 2, "sort_threads": args.sort_threads or 512,
-                "depth_sort_items": args.depth_sort_items or 16}
+                "depth_sort_items": args.depth_sort_items or 16, "depth_sort_threads": args.depth_sort_threads or 256}
     ms, st, _, _ = train_rate("cfg2", stream, 0, args.steps, args.warmup, settings)
     print(json.dumps({"fwd_bwd": {"config": "cfg2", "value": round(1000.0 / ms, 3), "unit": "it/s",
                                   "ms_per_step": round(ms, 4), "keys": int(st["keys"]), "settings": settings}}))
@@ -369,7 +369,8 @@ def run_ours(args):
 
     if args.sort_ctas:
         settings, tuned = {"sort_ctas_per_sm": args.sort_ctas, "sort_threads": args.sort_threads,
-                           "depth_sort_items": args.depth_sort_items}, None
+                           "depth_sort_items": args.depth_sort_items,
+                           "depth_sort_threads": args.depth_sort_threads}, None
     else:
         from torpedo_gb300 import autotune
 
@@ -548,6 +549,7 @@ def main():
                     help="radix pass kernel residency (2 or 3 CTAs per SM); 0 = autotune")
     ap.add_argument("--sort-threads", type=int, default=0, help="with --sort-ctas: radix CTA size (256 or 512)")
     ap.add_argument("--depth-sort-items", type=int, default=0, help="with --sort-ctas: depth sort keys per thread")
+    ap.add_argument("--depth-sort-threads", type=int, default=0, help="with --sort-ctas: depth sort CTA size (256 or 512)")
     ap.add_argument("--no-train", action="store_true", help="skip the cfg2 and cfg3 forward+backward measurements")
     ap.add_argument("--train-only", action="store_true", help="only the cfg2 forward+backward steps (profiling)")
     args = ap.parse_args()

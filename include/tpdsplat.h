@@ -66,10 +66,12 @@ typedef struct tpd_settings {
     double timeout_s;              /* host wait limit per frame in seconds (0: 60) */
     uint32_t test_never_publish;   /* test hook: scan partition 0 never publishes (exercises the bounded spin) */
     uint32_t stage_timing;         /* 1: frames run without a graph and record CUDA events between stages */
-    uint32_t sort_ctas_per_sm;     /* radix pass kernel residency: 3 (0 = default) or 2 (no register spills) */
-    uint32_t depth_sort_items;     /* keys per thread of the depth sort's radix passes: 4, 8 or 16 (0 = default 8) */
-    uint32_t sort_threads;         /* radix pass CTA size for 4096-key partitions: 256 (0 = default) or 512 (8 keys each) */
-    uint32_t reserved[3];
+    uint32_t sort_ctas_per_sm;     /* residency of the 256 x 16-key radix pass kernel: 2 (0 = default, no register spills) or 3 */
+    uint32_t depth_sort_items;     /* keys per thread of the depth sort's 256-thread radix passes: 16 (0 = default), 8 or 4 */
+    uint32_t sort_threads;         /* CTA size of the key sort's 4096-key radix passes: 512 x 8 keys (0 = default) or 256 x 16 */
+    uint32_t depth_sort_threads;   /* CTA size of the depth sort's radix passes: 256 (0 = default) or 512 (8 keys each,
+                                      whatever depth_sort_items says) */
+    uint32_t reserved[2];
 } tpd_settings;
 
 /* Stages of a frame, for tpd_stage_times. */

@@ -32,7 +32,8 @@ class Settings(C.Structure):
         ("sort_ctas_per_sm", C.c_uint32),
         ("depth_sort_items", C.c_uint32),
         ("sort_threads", C.c_uint32),
-        ("reserved", C.c_uint32 * 3),
+        ("depth_sort_threads", C.c_uint32),
+        ("reserved", C.c_uint32 * 2),
     ]
 
 

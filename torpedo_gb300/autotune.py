@@ -6,13 +6,15 @@ fastest, one axis at a time (each axis tried with the best values found so
 far for the others). The tunables are engine settings that leave every
 result bit for bit unchanged:
 
-  sort_threads       CTA size of the 4096-key radix passes: 256 threads x 16
-                     keys, or 512 threads x 8 keys (twice the warps per SM)
-  sort_ctas_per_sm   residency the 256-thread radix pass kernel is compiled
-                     for (2: 128 registers, no spills; 3: 80 registers)
-  depth_sort_items   keys per thread of the depth sort's radix passes (4, 8,
-                     16: partitions of 1024, 2048, 4096 keys); smaller
+  sort_threads       CTA size of the key sort's 4096-key radix passes: 512
+                     threads x 8 keys (digits ranked with match-any, twice the
+                     warps per SM) or 256 threads x 16 keys (bit ballots)
+  depth_sort_threads the same choice for the depth sort's passes
+  depth_sort_items   keys per thread of the depth sort's 256-thread passes
+                     (16, 8, 4: partitions of 4096, 2048, 1024 keys); smaller
                      partitions fill the GPU when the Gaussians are few
+  sort_ctas_per_sm   residency the 256 x 16-key pass kernel is compiled for
+                     (2: 128 registers, no spills; 3: 80 registers)
 
 The tile size stays 16x16 and the radix digit 8 bits: the tile size fixes
 the reference's key layout (tile id | depth), and a 13-bit tile id takes two
@@ -22,7 +24,8 @@ from __future__ import annotations
 
 from typing import Callable
 
-AXES = (("sort_threads", (256, 512)), ("sort_ctas_per_sm", (2, 3)), ("depth_sort_items", (16, 8)))
+AXES = (("sort_threads", (512, 256)), ("depth_sort_threads", (256, 512)), ("depth_sort_items", (16, 8)),
+        ("sort_ctas_per_sm", (2, 3)))
 
 
 def time_steps(make_engine: Callable[[dict], object], enqueue: Callable[[object, int], None], stream,

@@ -344,8 +344,8 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     dp.ticket_base = kTicketDepthSortBase;
     dp.tag_base = kTagDepthSort;
     dp.ctas_per_sm = int(e->settings.sort_ctas_per_sm);
-    dp.items = e->settings.depth_sort_items == 4 || e->settings.depth_sort_items == 16 ? e->settings.depth_sort_items : 8;
-    dp.threads = e->settings.sort_threads == 512 ? 512 : 256;
+    dp.items = e->settings.depth_sort_items == 4 || e->settings.depth_sort_items == 8 ? e->settings.depth_sort_items : 16;
+    dp.threads = e->settings.depth_sort_threads == 512 ? 512 : 256;
     dp.fixed_count = items;
     e->depth_in_alt = launch_sort(e->d_dkeys[0], e->d_ditems[0], e->d_dkeys[1], e->d_ditems[1], items, dp,
                                   e->d_desc_depth, e->d_ctl, spin, e->num_sms, s);
@@ -365,7 +365,7 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     kp.ticket_base = kTicketKeySortBase;
     kp.tag_base = kTagKeySort;
     kp.ctas_per_sm = int(e->settings.sort_ctas_per_sm);
-    kp.threads = e->settings.sort_threads == 512 ? 512 : 256;
+    kp.threads = e->settings.sort_threads == 256 ? 256 : 512;
     kp.ranges = e->d_ranges;  // the last pass writes the tile ranges
     kp.n_tiles = e->total_tiles;
     e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, kp, e->d_desc_sort,

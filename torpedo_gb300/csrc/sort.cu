@@ -151,7 +151,7 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
         const int cnt = p >= 3 ? 4 : int(p) + 1;
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-            if (j < cnt) d[j] = TPD_INBOUNDS(ctl, 10, uint64_t(p - j), part) ? ld_relaxed_u64(desc + size_t(p - j) * kRadix + digit) : make_desc(kFlagPrefix, tag, 0);
+            if (j < cnt) d[j] = ld_relaxed_u64(desc + size_t(p - j) * kRadix + digit);  // 0 <= p - j < part
         bool stop = false, wait = false;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -214,6 +214,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     uint32_t spin_limit, uint32_t* __restrict__ ranges, uint32_t n_tiles) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr uint32_t kSortItems = kItems, kSortTile = kThreads * kItems, kWarps = kThreads / 32;
+    // digits ranked with match-any in the 512-thread variant (32 warps per SM
+    // hide its latency), with bit ballots otherwise (fixed cost)
+    constexpr bool kMatchRank = kThreads == 512;
     OnesweepSmem<kItems, kThreads>& S = *reinterpret_cast<OnesweepSmem<kItems, kThreads>*>(smem_raw);
     const bool digit_thread = threadIdx.x < kRadix;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -260,21 +263,26 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         for (uint32_t i = 0; i < kSortItems; ++i) {
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
             const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
-            // lanes with the same digit: one ballot per digit bit (the pass's
-            // `bits`, plus bit 8 for the past-the-end digit)
-            uint32_t peers = 0xFFFFFFFFu;
+            uint32_t peers;
+            if constexpr (kMatchRank) {
+                peers = __match_any_sync(0xFFFFFFFFu, d);
+            } else {
+                // lanes with the same digit: one ballot per digit bit (bits
+                // above the pass's width are zero in every valid lane and
+                // leave the mask as it is), and one for the past-the-end digit
+                // in the partition that has any
+                peers = 0xFFFFFFFFu;
 #pragma unroll
-            for (uint32_t b = 0; b < kRadixBits; ++b) {
-                if (b < bits) {
+                for (uint32_t b = 0; b < kRadixBits; ++b) {
                     const bool on = (d >> b) & 1u;
                     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
                     peers &= on ? bal : ~bal;
                 }
-            }
-            {
-                const bool on = d >= kRadix;
-                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
-                peers &= on ? bal : ~bal;
+                if (cnt < kSortTile) {
+                    const bool on = d >= kRadix;
+                    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+                    peers &= on ? bal : ~bal;
+                }
             }
             const uint32_t leader = __ffs(peers) - 1;
             uint32_t prev = 0;
@@ -418,14 +426,14 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
         sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, p0, p1, plan.key_bits, hist, ctl);
     }
     if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
-    if (plan.items == 8)
+    if (plan.threads == 512)
+        launch_passes<8, 512, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
+                                 sms, s);
+    else if (plan.items == 8)
         launch_passes<8, 256, 4>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
                                  sms, s);
     else if (plan.items == 4)
         launch_passes<4, 256, 5>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
-                                 sms, s);
-    else if (plan.threads == 512)
-        launch_passes<8, 512, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
                                  sms, s);
     else if (plan.ctas_per_sm == 3)
         launch_passes<16, 256, 3>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,

@@ -100,7 +100,7 @@ struct SortPlan {
     uint32_t tag_base = kTagKeySort;
     int ctas_per_sm = 2;
     uint32_t items = 16;               // keys per thread: 16 (4096-key partitions), 8 or 4
-    uint32_t threads = 256;            // 512: 4096-key partitions as 512 threads x 8 keys (items 16 only)
+    uint32_t threads = 256;            // 512: 4096-key partitions as 512 threads x 8 keys (items unused)
     uint32_t* ranges = nullptr;        // key sort: the last pass also writes the tile ranges (preset by keygen)
     uint32_t n_tiles = 0;
     uint32_t fixed_count = 0;          // nonzero: sort this many pairs, else min(ctl->total_keys, capacity)

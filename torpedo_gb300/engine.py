@@ -150,7 +150,7 @@ class GaussianEngine:
     def __init__(self, sh_degree: int = 3, band3_compat: bool = True, device: int = 0, stream: int | None = None,
                  use_graph: bool = True, spin_limit: int = 0, initial_key_capacity: int = 0, timeout_s: float = 60.0,
                  test_never_publish: bool = False, stage_timing: bool = False, sort_ctas_per_sm: int = 0,
-                 depth_sort_items: int = 0, sort_threads: int = 0):
+                 depth_sort_items: int = 0, sort_threads: int = 0, depth_sort_threads: int = 0):
         lib = L.load()
         s = L.Settings()
         lib.tpd_settings_init(C.byref(s))
@@ -167,6 +167,7 @@ class GaussianEngine:
         s.sort_ctas_per_sm = sort_ctas_per_sm
         s.depth_sort_items = depth_sort_items
         s.sort_threads = sort_threads
+        s.depth_sort_threads = depth_sort_threads
         h = C.c_void_p()
         _check(lib.tpd_create(C.byref(s), C.byref(h)))
         self._h = h
