@@ -232,31 +232,49 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         if (digit_thread) S.gdig[tid] = ex;
     }
 
-    while (true) {
-        if (tid == 0) S.part = atomicAdd(&ctl->ticket[ticket_slot], 1u);
-#pragma unroll
-        for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
-        __syncthreads();
-        const uint32_t part = S.part;
-        if (part >= nparts) break;
-        const uint32_t base = part * kSortTile;
-        const uint32_t cnt = min(kSortTile, K - base);
-
-        // Warp-striped items, loaded coalesced straight from global memory: warp
-        // w owns [w*512, w*512+512), item i covers 32 consecutive keys. dr[i]
-        // packs the digit (bits 0..8, kInvalidDigit past K) and the key's rank
-        // among equal digits earlier in the warp (bits 9..31).
-        uint64_t k[kSortItems];
-        // variants with registers to spare load the values with the keys, so
-        // the two loads share one memory latency
-        constexpr bool kValsEarly = kItems * kMinBlocks * (kThreads / 256) <= 32;
-        uint32_t vr[kValsEarly ? kSortItems : 1];
+    // Warp-striped items, loaded coalesced straight from global memory: warp w
+    // owns [w*32*kItems, (w+1)*32*kItems), item i covers 32 consecutive keys.
+    // Variants with registers to spare load the values with the keys. The
+    // 256-thread variants load a CTA's next partition while they write out the
+    // current one (thread 0 takes its ticket after its look-back), hiding the
+    // load latency behind the write-out; the 512-thread variant, at 64
+    // registers, takes its ticket and loads at the top of each partition.
+    constexpr bool kValsEarly = kItems * kMinBlocks * (kThreads / 256) <= 32;
+    constexpr bool kPrefetch = kThreads == 256;
+    uint64_t k[kSortItems];
+    uint32_t vr[kValsEarly ? kSortItems : 1];
+    auto load_partition = [&](uint32_t p) {
+        const uint32_t b = p * kSortTile, c = p < nparts ? min(kSortTile, K - b) : 0u;
 #pragma unroll
         for (uint32_t i = 0; i < kSortItems; ++i) {
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-            k[i] = idx < cnt ? keys_in[base + idx] : ~0ull;
-            if constexpr (kValsEarly) vr[i] = idx < cnt ? vals_in[base + idx] : 0u;
+            k[i] = idx < c ? keys_in[b + idx] : ~0ull;
+            if constexpr (kValsEarly) vr[i] = idx < c ? vals_in[b + idx] : 0u;
         }
+    };
+    uint32_t part = 0;
+    if constexpr (kPrefetch) {
+        if (tid == 0) S.part = atomicAdd(&ctl->ticket[ticket_slot], 1u);
+        __syncthreads();
+        part = S.part;
+        load_partition(part);
+    }
+
+    while (true) {
+        if constexpr (!kPrefetch) {
+            if (tid == 0) S.part = atomicAdd(&ctl->ticket[ticket_slot], 1u);
+        }
+#pragma unroll
+        for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
+        __syncthreads();
+        if constexpr (!kPrefetch) part = S.part;
+        if (part >= nparts) break;
+        if constexpr (!kPrefetch) load_partition(part);
+        const uint32_t base = part * kSortTile;
+        const uint32_t cnt = min(kSortTile, K - base);
+
+        // dr[i] packs the digit (bits 0..8, kInvalidDigit past K) and the
+        // key's rank among equal digits earlier in the warp (bits 9..31).
         uint32_t dr[kSortItems];
         const uint32_t lt = lanemask_lt();
 #pragma unroll
@@ -336,7 +354,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             }
         }
 
-        // decoupled look-back for this thread's digit
+        // decoupled look-back for this thread's digit; then (prefetching
+        // variants) thread 0 takes the next partition's ticket: every thread
+        // has read S.part since it was last written
         if (digit_thread) {
             if (part > 0) {
                 const uint32_t excl = digit_lookback(desc, part, tid, tag, ctl, spin_limit);
@@ -346,7 +366,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 S.gmap[tid] = S.gdig[tid] - lstart;
             }
         }
+        if constexpr (kPrefetch) {
+            if (tid == 0) S.part = atomicAdd(&ctl->ticket[ticket_slot], 1u);
+        }
         __syncthreads();
+        if constexpr (kPrefetch) {
+            part = S.part;
+            load_partition(part);  // k and vr are free since the reorder
+        }
 
         // coalesced write-out of digit runs
         for (uint32_t j = tid; j < cnt; j += kThreads) {
