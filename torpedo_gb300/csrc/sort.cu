@@ -224,6 +224,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
     const uint32_t tag = ctl->tag * 32u + tag_slot;
     const uint32_t mask = (1u << bits) - 1u;
+    // digits of this pass's width: only these count, publish and look back
+    // (a 5-bit pass leaves 224 of the 256 digit threads idle)
+    const bool live_digit = tid <= mask;
 
     // global exclusive digit offsets (histogram of this pass, scanned)
     {
@@ -317,7 +320,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         // per digit (thread = digit): warp prefixes, block count, local start
         uint32_t count = 0;
         uint64_t* dp = nullptr;
-        if (digit_thread) {
+        if (live_digit) {
 #pragma unroll
             for (uint32_t w = 0; w < kWarps; ++w) {
                 const uint32_t c = S.whist[w][tid];
@@ -357,7 +360,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         // decoupled look-back for this thread's digit; then (prefetching
         // variants) thread 0 takes the next partition's ticket: every thread
         // has read S.part since it was last written
-        if (digit_thread) {
+        if (live_digit) {
             if (part > 0) {
                 const uint32_t excl = digit_lookback(desc, part, tid, tag, ctl, spin_limit);
                 st_relaxed_u64(dp, make_desc(kFlagPrefix, tag, excl + count));
