@@ -335,25 +335,39 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         __syncthreads();
 
         // reorder the partition in shared memory (stable: warp, then item, then
-        // lane) while predecessors publish; values are loaded now, coalesced
+        // lane) while predecessors publish; values not held in registers are
+        // loaded now, coalesced
+        if constexpr (kValsEarly) {
+            // key and value go to the same slot: one position per item
 #pragma unroll
-        for (uint32_t i = 0; i < kSortItems; ++i) {
-            const uint32_t d = dr[i] & 511u;
-            if (d < kRadix) {
-                const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-                if (TPD_INBOUNDS(ctl, 11, pos, cnt)) S.keys[pad16(pos)] = k[i];
+            for (uint32_t i = 0; i < kSortItems; ++i) {
+                const uint32_t d = dr[i] & 511u;
+                if (d < kRadix) {
+                    const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                    if (TPD_INBOUNDS(ctl, 11, pos, cnt)) {
+                        S.keys[pad16(pos)] = k[i];
+                        S.vals[pad16(pos)] = vr[i];
+                    }
+                }
             }
-        }
+        } else {
 #pragma unroll
-        for (uint32_t i = 0; i < kSortItems; ++i) {
-            const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-            const uint32_t d = dr[i] & 511u;
-            if (d < kRadix) {
-                uint32_t v;
-                if constexpr (kValsEarly) v = vr[i];
-                else v = vals_in[base + idx];
-                const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-                if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pad16(pos)] = v;
+            for (uint32_t i = 0; i < kSortItems; ++i) {
+                const uint32_t d = dr[i] & 511u;
+                if (d < kRadix) {
+                    const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                    if (TPD_INBOUNDS(ctl, 11, pos, cnt)) S.keys[pad16(pos)] = k[i];
+                }
+            }
+#pragma unroll
+            for (uint32_t i = 0; i < kSortItems; ++i) {
+                const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
+                const uint32_t d = dr[i] & 511u;
+                if (d < kRadix) {
+                    const uint32_t v = vals_in[base + idx];
+                    const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                    if (TPD_INBOUNDS(ctl, 12, pos, cnt)) S.vals[pad16(pos)] = v;
+                }
             }
         }
 
