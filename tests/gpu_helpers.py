@@ -54,7 +54,8 @@ def oracle_frame(records, cam, sh_degree=3, band3_compat=True, ent_idx=None, tra
     n_tiles = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
     rng = O.tile_ranges(skeys, n_tiles)
     # key offsets in depth order (the engine scans tile counts after sorting the
-    # Gaussians by (depth bits, index); culled ones, depth key 0xFFFFFFFF, go last)
+    # Gaussians by (depth bits, index); culled ones, depth key 0xFFFFFFFF, go
+    # last here and are dropped by the engine's depth sort)
     dkey = np.where(s32[:, 3] > 0, s32[:, 6], np.uint32(0xFFFFFFFF)).astype(np.uint32)
     order = np.argsort(dkey, kind="stable")
     cnt = s32[order, 3].astype(np.uint64)

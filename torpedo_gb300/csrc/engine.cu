@@ -347,6 +347,7 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     dp.items = e->settings.depth_sort_items == 4 || e->settings.depth_sort_items == 8 ? e->settings.depth_sort_items : 16;
     dp.threads = e->settings.depth_sort_threads == 512 ? 512 : 256;
     dp.fixed_count = items;
+    dp.compact_culled = true;  // culled items leave in the first pass; the rest sort ctl->depth_count
     e->depth_in_alt = launch_sort(e->d_dkeys[0], e->d_ditems[0], e->d_dkeys[1], e->d_ditems[1], items, dp,
                                   e->d_desc_depth, e->d_ctl, spin, e->num_sms, s);
     const uint32_t* order = e->d_ditems[e->depth_in_alt ? 1 : 0];

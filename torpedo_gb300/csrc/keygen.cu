@@ -22,8 +22,9 @@ namespace {
 
 constexpr uint32_t kKeygenThreads = 256;
 
-// Walks the (view, Gaussian) items in depth order (items[r] = v * n + i, their
-// key offsets in offsets[r]); a warp owns 32 consecutive items, whose keys
+// Walks the ctl->depth_count (view, Gaussian) items the depth sort kept, in
+// depth order (items[r] = v * n + i < n_items, their key offsets in
+// offsets[r]); a warp owns 32 consecutive items, whose keys
 // are contiguous, and produces them in windows of kKeyWindow output slots:
 //  1. each lane with keys marks its first slot in the window's owner map,
 //     a prefix-max over the map gives every slot its owning lane;
@@ -51,7 +52,7 @@ struct KeygenSmem {
 
 __global__ void __launch_bounds__(kKeygenThreads)
     keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
-                  const uint32_t* __restrict__ offsets, uint32_t count, uint32_t n,
+                  const uint32_t* __restrict__ offsets, uint32_t n_items, uint32_t n,
                   const ViewConst* __restrict__ views, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                   uint32_t capacity, uint32_t key_bits, uint32_t* __restrict__ ranges, uint32_t n_tiles,
                   FrameCtl* ctl) {
@@ -61,6 +62,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
     const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
     if (ctl->status & kStatusFatal) return;
+    const uint32_t count = min(ctl->depth_count, n_items);
     const uint32_t npass = min(8u, (key_bits + 7) / 8);
     // ranges: (0xFFFFFFFF, 0) until the key sort's last pass narrows them
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x)
@@ -78,8 +80,8 @@ __global__ void __launch_bounds__(kKeygenThreads)
         if (r < count) {
             const uint32_t item = items[r];
             off = offsets[r];
-            if (TPD_INBOUNDS(ctl, 21, item, count)) {
-                const uint32_t v = count == n ? 0u : item / n;  // one view: no division
+            if (TPD_INBOUNDS(ctl, 21, item, n_items)) {
+                const uint32_t v = n_items == n ? 0u : item / n;  // one view: no division
                 gi = item - v * n;
                 const ViewConst& vc = views[v];
                 gx = grid_x(vc.width);
@@ -185,11 +187,11 @@ __global__ void __launch_bounds__(kKeygenThreads)
 
 }  // namespace
 
-void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t count, uint32_t n,
+void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
                    const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
                    uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s) {
-    if (count == 0 || n == 0) return;
-    const uint64_t warps = (uint64_t(count) + 31) / 32;
+    if (n_items == 0 || n == 0) return;
+    const uint64_t warps = (uint64_t(n_items) + 31) / 32;
     uint64_t blocks = (warps * 32 + kKeygenThreads - 1) / kKeygenThreads;
     static int per_sm = 0;  // resident CTAs per SM (shared memory bound)
     if (per_sm == 0) {
@@ -199,7 +201,7 @@ void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* o
     }
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
     blocks = blocks < cap ? blocks : cap;
-    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, count, n, views, keys, vals,
+    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, n_items, n, views, keys, vals,
                                                               capacity, key_bits, ranges, n_tiles, ctl);
 }
 

@@ -76,6 +76,7 @@ __global__ void frame_begin_kernel(FrameCtl* ctl, const float* transforms, uint3
         ctl->status = 0;
         ctl->total_keys = 0;
         ctl->visible = 0;
+        ctl->depth_count = 0;
     }
     if (!views || !ent_mats) return;
     for (uint32_t ve = t; ve < n_views * n_ent; ve += blockDim.x) {
@@ -245,6 +246,7 @@ struct PreSmem {
     float rec[kPreStages][kPreThreads * kRecordFloats];  // 30,720 B per stage, 16-byte multiple
     uint32_t hist[kDepthPassesMax][256];                  // depth-key digit counts of this CTA
     uint64_t bar[kPreStages];
+    uint32_t kept;                                        // depth keys of visible items in this CTA
 };
 
 __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs a) {
@@ -253,6 +255,8 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
 
     const uint32_t tid = threadIdx.x;
     for (uint32_t k = tid; k < kDepthPassesMax * 256; k += kPreThreads) (&S.hist[0][0])[k] = 0;
+    if (tid == 0) S.kept = 0;
+    uint32_t kept = 0;  // this thread's visible items (the depth sort drops the others)
     if (tid == 0) {
         for (uint32_t st = 0; st < kPreStages; ++st) mbar_init(&S.bar[st], 1);
         fence_mbar_init();
@@ -301,12 +305,16 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
                 dst[1] = src[1];
                 dst[2] = src[2];
                 if (a.depth_keys) {
+                    // culled: low 32 bits 0xFFFFFFFF, dropped by the depth sort's first pass
                     const uint64_t key = (uint64_t(v) << 32) | (tiles ? __float_as_uint(sp.depth) : 0xFFFFFFFFu);
                     a.depth_keys[item] = key;
                     a.depth_items[item] = uint32_t(item);
-                    for (uint32_t p = 0; p < npass; ++p) {
-                        const uint32_t bits = min(8u, a.depth_key_bits - 8 * p);
-                        atomicAdd(&S.hist[p][uint32_t(key >> (8 * p)) & ((1u << bits) - 1u)], 1u);
+                    if (tiles) {
+                        ++kept;
+                        for (uint32_t p = 0; p < npass; ++p) {
+                            const uint32_t bits = min(8u, a.depth_key_bits - 8 * p);
+                            atomicAdd(&S.hist[p][uint32_t(key >> (8 * p)) & ((1u << bits) - 1u)], 1u);
+                        }
                     }
                 }
             }
@@ -314,6 +322,10 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
         __syncthreads();  // every thread is done with this stage before it is refilled
     }
     if (!a.depth_keys) return;
+    kept = warp_sum(kept);
+    if ((tid & 31u) == 0 && kept) atomicAdd(&S.kept, kept);
+    __syncthreads();
+    if (tid == 0 && S.kept) atomicAdd(&a.ctl->depth_count, S.kept);
     for (uint32_t p = 0; p < npass; ++p)
         for (uint32_t d = tid; d < 256; d += kPreThreads)
             if (S.hist[p][d]) atomicAdd(&a.ctl->depth_hist[p][d], S.hist[p][d]);
@@ -326,18 +338,22 @@ constexpr uint32_t kScanThreads = 256;
 
 // kItems consecutive items per thread: 4 for the standalone scan, 16 for the
 // depth-order scan of the frame (4096-item partitions: a quarter of the
-// look-back chain; the item indices are read 16 bytes at a time).
+// look-back chain; the item indices are read 16 bytes at a time). The
+// depth-order scan covers the ctl->depth_count items the depth sort kept
+// (at most n): the grid is sized for n and the partitions past the count exit.
 template <bool kGather, uint32_t kItems>
 __global__ void __launch_bounds__(kScanThreads)
-    scan_tiles_kernel(const Splat* splats, const uint32_t* items, uint32_t n, uint32_t* offsets, uint64_t* desc,
+    scan_tiles_kernel(const Splat* splats, const uint32_t* items, uint32_t n_max, uint32_t* offsets, uint64_t* desc,
                       FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish) {
     constexpr uint32_t kScanTile = kScanThreads * kItems;
     __shared__ uint32_t s_part, s_excl;
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t n = kGather ? min(ctl->depth_count, n_max) : n_max;
     if (tid == 0) s_part = atomicAdd(&ctl->ticket[kTicketScan], 1u);
     __syncthreads();
     const uint32_t part = s_part;
+    if (part * kScanTile >= n) return;  // (uniform) past the items; nothing waits on it
     const uint32_t base = part * kScanTile + tid * kItems;
     uint32_t it[kItems];
     if constexpr (kGather && kItems % 4 == 0) {
@@ -441,12 +457,12 @@ void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint6
                                                                 never_publish);
 }
 
-void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t count, uint32_t* offsets, uint64_t* desc,
-                       FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
-    if (count == 0) return;
-    const uint32_t blocks = (count + kScanThreads * 16 - 1) / (kScanThreads * 16);
-    scan_tiles_kernel<true, 16><<<blocks, kScanThreads, 0, s>>>(splats, items, count, offsets, desc, ctl, spin_limit,
-                                                                never_publish);
+void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t max_count, uint32_t* offsets,
+                       uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
+    if (max_count == 0) return;
+    const uint32_t blocks = (max_count + kScanThreads * 16 - 1) / (kScanThreads * 16);
+    scan_tiles_kernel<true, 16><<<blocks, kScanThreads, 0, s>>>(splats, items, max_count, offsets, desc, ctl,
+                                                                spin_limit, never_publish);
 }
 
 void launch_pack_records(const float* means, const float* log_scales, const float* quats, const float* logits,

@@ -40,7 +40,14 @@ constexpr uint32_t kSortWarps = kSortThreads / 32;
 // GPU with 4096-key partitions (the depth sort of 1M Gaussians).
 constexpr uint32_t kSortItemsMax = 16;
 constexpr uint32_t kSortTileMax = kSortThreads * kSortItemsMax;
-constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K
+constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K (and dropped keys)
+
+// Pass kinds of onesweep_kernel. The depth sort compacts the culled items
+// away in its first pass and sorts the remaining ctl->depth_count items in
+// the others, where a pass whose digit is the same for every key is a copy.
+constexpr int kPassPlain = 0;      // K = fixed_count, else ctl->total_keys
+constexpr int kPassDropCulled = 1; // as plain; keys whose low 32 bits are 0xFFFFFFFF are not written
+constexpr int kPassCompacted = 2;  // K = ctl->depth_count; a uniform digit makes the pass a copy
 
 constexpr uint32_t kHistThreads = 256;
 constexpr uint32_t kHistChunk = 2048;  // keys per TMA chunk (16 KB)
@@ -62,6 +69,7 @@ struct OnesweepSmem {
     uint32_t gmap[kRadix];    // global position of local index 0 of each digit
     uint32_t wsum[kThreads / 32];
     uint32_t part;
+    uint32_t valid;  // keys of the partition that are written (all but dropped ones)
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -204,8 +212,9 @@ __device__ __forceinline__ void tile_range_bounds(const OnesweepSmem<kItems, kTh
 }
 
 // kThreads = 256 (one digit per thread) or 512 (the digit-wide steps run on
-// the first 256 threads); a partition is kThreads * kItems keys.
-template <int kItems, int kThreads, int kMinBlocks>
+// the first 256 threads); a partition is kThreads * kItems keys. kPass is a
+// pass kind (kPassPlain ...): dropped keys are ranked as past-the-end keys.
+template <int kItems, int kThreads, int kMinBlocks, int kPass>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
@@ -220,7 +229,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     OnesweepSmem<kItems, kThreads>& S = *reinterpret_cast<OnesweepSmem<kItems, kThreads>*>(smem_raw);
     const bool digit_thread = threadIdx.x < kRadix;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t K = (ctl->status & kStatusFatal) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
+    constexpr bool kDrop = kPass == kPassDropCulled;
+    const uint32_t K = (ctl->status & kStatusFatal)
+                           ? 0u
+                           : min(kPass == kPassCompacted ? ctl->depth_count
+                                                         : (fixed_count ? fixed_count : ctl->total_keys),
+                                 capacity);
     const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
     const uint32_t tag = ctl->tag * 32u + tag_slot;
     const uint32_t mask = (1u << bits) - 1u;
@@ -229,10 +243,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const bool live_digit = tid <= mask;
 
     // global exclusive digit offsets (histogram of this pass, scanned)
+    const uint32_t h = digit_thread && TPD_INBOUNDS(ctl, 16, pass, 8) ? hist[pass][tid] : 0u;
     {
-        const uint32_t h = digit_thread && TPD_INBOUNDS(ctl, 16, pass, 8) ? hist[pass][tid] : 0u;
         const uint32_t ex = block_exclusive_scan256<kWarps>(h, S.wsum);
         if (digit_thread) S.gdig[tid] = ex;
+    }
+    if constexpr (kPass == kPassCompacted) {
+        // a pass whose digit is the same for all K keys leaves their order as
+        // it is: the grid copies them
+        if (__syncthreads_or(digit_thread && K > 0 && h == K)) {
+            for (uint32_t i = blockIdx.x * kThreads + tid; i < K; i += gridDim.x * kThreads) {
+                keys_out[i] = keys_in[i];
+                vals_out[i] = vals_in[i];
+            }
+            return;
+        }
     }
 
     // Warp-striped items, loaded coalesced straight from global memory: warp w
@@ -283,15 +308,16 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 #pragma unroll
         for (uint32_t i = 0; i < kSortItems; ++i) {
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-            const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
+            const uint32_t d = idx < cnt && !(kDrop && uint32_t(k[i]) == 0xFFFFFFFFu) ? (uint32_t(k[i] >> shift) & mask)
+                                                                                     : kInvalidDigit;
             uint32_t peers;
             if constexpr (kMatchRank) {
                 peers = __match_any_sync(0xFFFFFFFFu, d);
             } else {
                 // lanes with the same digit: one ballot per digit bit (bits
                 // above the pass's width are zero in every valid lane and
-                // leave the mask as it is), and one for the past-the-end digit
-                // in the partition that has any
+                // leave the mask as it is), and one for the past-the-end (or
+                // dropped) digit in the partitions that can have any
                 peers = 0xFFFFFFFFu;
 #pragma unroll
                 for (uint32_t b = 0; b < kRadixBits; ++b) {
@@ -299,7 +325,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
                     peers &= on ? bal : ~bal;
                 }
-                if (cnt < kSortTile) {
+                if (kDrop || cnt < kSortTile) {
                     const bool on = d >= kRadix;
                     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
                     peers &= on ? bal : ~bal;
@@ -332,6 +358,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         }
         const uint32_t lstart = block_exclusive_scan256<kWarps>(count, S.wsum);  // (its barriers cover whist)
         if (digit_thread) S.lstart[tid] = lstart;
+        if (kDrop && tid == kRadix - 1) S.valid = lstart + count;
         __syncthreads();
 
         // reorder the partition in shared memory (stable: warp, then item, then
@@ -393,14 +420,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         }
 
         // coalesced write-out of digit runs
-        for (uint32_t j = tid; j < cnt; j += kThreads) {
+        const uint32_t cntv = kDrop ? S.valid : cnt;
+        for (uint32_t j = tid; j < cntv; j += kThreads) {
             const uint64_t key = S.keys[pad16(j)];
             const uint32_t d = uint32_t(key >> shift) & mask;
             const uint32_t g = S.gmap[d] + j;
             if (g < capacity && TPD_INBOUNDS(ctl, 17, g, K + (K == 0))) {
                 keys_out[g] = key;
                 vals_out[g] = S.vals[pad16(j)];
-                if (ranges) tile_range_bounds(S, ranges, n_tiles, key, j, cnt, d, g, shift, mask, ctl);
+                if (ranges) tile_range_bounds(S, ranges, n_tiles, key, j, cntv, d, g, shift, mask, ctl);
             }
         }
         __syncthreads();  // S.keys / S.vals / S.gmap are rewritten by the next partition
@@ -416,11 +444,15 @@ int onesweep_occupancy() {
     static int b = 0;
     if (b == 0) {
         const size_t smem = sizeof(OnesweepSmem<kItems, kThreads>);
-        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks>,
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         int r = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kThreads, kMinBlocks>, kThreads,
-                                                      smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain>,
+                                                      kThreads, smem);
         b = r > 0 ? r : 1;
     }
     return b;
@@ -438,9 +470,12 @@ void launch_passes(uint64_t* kin, uint32_t* vin, uint64_t* kout, uint32_t* vout,
     for (uint32_t p = p0; p < p1; ++p) {
         const uint32_t shift = p * kRadixBits;
         const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
-        onesweep_kernel<kItems, kThreads, kMinBlocks><<<grid, kThreads, smem, s>>>(
-            kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p, plan.tag_base + p,
-            plan.fixed_count, desc, ctl, spin_limit, p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles);
+        auto kernel = !plan.compact_culled ? onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain>
+                      : p == p0            ? onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled>
+                                           : onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted>;
+        kernel<<<grid, kThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p,
+                                            plan.tag_base + p, plan.fixed_count, desc, ctl, spin_limit,
+                                            p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

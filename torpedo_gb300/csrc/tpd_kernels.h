@@ -21,7 +21,8 @@ struct FrameCtl {
     uint32_t sort_hist[8][256];   // digit counts of the key sort, by 8-bit digit position
     uint32_t depth_hist[8][256];  // digit counts of the depth sort, by 8-bit digit position
     uint32_t debug[4];       // site, index, bound of the first failed index guard
-    uint32_t pad[4];
+    uint32_t depth_count;    // (view, Gaussian) items with a non-empty tile rect: those the depth sort keeps
+    uint32_t pad[3];
 };
 
 // Entity matrices: rows 0..2 of view*model and rows 0..3 of projview*model.
@@ -63,11 +64,12 @@ void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, 
                         uint32_t n_views, float* ent_mats, cudaStream_t s);
 void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s);
 
-// Tile counts of (view, Gaussian) items in depth order, gathered through
-// items[r] = v * n + i, scanned into exclusive key offsets offsets[r]; the total
-// goes to ctl->total_keys and the non-empty count to ctl->visible.
-void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t count, uint32_t* offsets, uint64_t* desc,
-                       FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s);
+// Tile counts of the ctl->depth_count (view, Gaussian) items in depth order
+// (at most max_count), gathered through items[r] = v * n + i, scanned into
+// exclusive key offsets offsets[r]; the total goes to ctl->total_keys and the
+// non-empty count to ctl->visible.
+void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t max_count, uint32_t* offsets,
+                       uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s);
 
 // Standalone exclusive scan of Splat.tiles (prefix.slang); total -> ctl->total_keys.
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
@@ -78,7 +80,8 @@ void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint6
 // ctl->total_keys; keys beyond capacity are dropped and flagged. Also counts the
 // digits of the tile-id passes (digit positions 4.. of key_bits) into ctl->sort_hist.
 // Also presets ranges (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
-void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t count, uint32_t n,
+// items[0 .. ctl->depth_count) index the n_items = n_views x n splats.
+void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
                    const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
                    uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s);
 
@@ -104,6 +107,10 @@ struct SortPlan {
     uint32_t* ranges = nullptr;        // key sort: the last pass also writes the tile ranges (preset by keygen)
     uint32_t n_tiles = 0;
     uint32_t fixed_count = 0;          // nonzero: sort this many pairs, else min(ctl->total_keys, capacity)
+    // depth sort: the first pass drops the keys whose low 32 bits are
+    // 0xFFFFFFFF (culled items) and keeps ctl->depth_count, which the later
+    // passes sort; a later pass whose digit is the same for every key copies
+    bool compact_culled = false;
     cudaEvent_t after_hist = nullptr;  // recorded between the histogram and the first pass
 };
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
