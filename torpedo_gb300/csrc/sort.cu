@@ -185,6 +185,33 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
     return excl;
 }
 
+// keys_out / vals_out [0, K) = keys_in / vals_in: thread t of nthr moves
+// 16-byte vectors (two keys, four values), kUnroll loads in flight before
+// their stores; scalar when a buffer is not 16-byte aligned.
+template <uint32_t kUnroll>
+__device__ __forceinline__ void copy_pairs(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                                           uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t K,
+                                           uint32_t t, uint32_t nthr) {
+    const bool vec = ((reinterpret_cast<uintptr_t>(keys_in) | reinterpret_cast<uintptr_t>(keys_out) |
+                       reinterpret_cast<uintptr_t>(vals_in) | reinterpret_cast<uintptr_t>(vals_out)) & 15u) == 0;
+    const uint32_t nk = vec ? K / 2 : 0u, nv = vec ? K / 4 : 0u;
+    auto copy16 = [&](const uint4* __restrict__ src, uint4* __restrict__ dst, uint32_t n) {
+        for (uint32_t i0 = t; i0 < n; i0 += nthr * kUnroll) {
+            uint4 r[kUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; ++u)
+                if (i0 + u * nthr < n) r[u] = src[i0 + u * nthr];
+#pragma unroll
+            for (uint32_t u = 0; u < kUnroll; ++u)
+                if (i0 + u * nthr < n) dst[i0 + u * nthr] = r[u];
+        }
+    };
+    copy16(reinterpret_cast<const uint4*>(keys_in), reinterpret_cast<uint4*>(keys_out), nk);
+    copy16(reinterpret_cast<const uint4*>(vals_in), reinterpret_cast<uint4*>(vals_out), nv);
+    for (uint32_t i = 2 * nk + t; i < K; i += nthr) keys_out[i] = keys_in[i];
+    for (uint32_t i = 4 * nv + t; i < K; i += nthr) vals_out[i] = vals_in[i];
+}
+
 // Tile ranges (range.slang:18-35) from the last pass of the key sort: the
 // partition's keys sit in shared memory fully sorted within each digit run,
 // and a digit run is contiguous in the output. A tile starts where the run's
@@ -252,10 +279,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         // a pass whose digit is the same for all K keys leaves their order as
         // it is: the grid copies them
         if (__syncthreads_or(digit_thread && K > 0 && h == K)) {
-            for (uint32_t i = blockIdx.x * kThreads + tid; i < K; i += gridDim.x * kThreads) {
-                keys_out[i] = keys_in[i];
-                vals_out[i] = vals_in[i];
-            }
+            copy_pairs<kItems >= 16 ? 8u : 4u>(keys_in, vals_in, keys_out, vals_out, K, blockIdx.x * kThreads + tid,
+                                               gridDim.x * kThreads);
             return;
         }
     }
