@@ -19,14 +19,16 @@
 // power/alpha are computed by one inline function with explicit rounding
 // intrinsics, so the forward and the adjoint take identical decisions.
 //
-// Warp culling: a warp owns an 8x4 pixel block of the tile. Each staged entry
-// carries the axis-aligned box of the ellipse on which alpha >= 1/255 can hold
-// (enlarged by a relative 2e-3 and 0.01 px); a warp ballots 32 entries at a
-// time against its block (box first, then the ellipse itself: the maximum of
-// p2 over the block) and walks only the entries that can reach it. A culled
-// pair lies outside that ellipse, where the exact alpha is below 1/255 and
-// the reference skips it too. Forward and adjoint use the same blocks and
-// tests, so they cull the same pairs.
+// Warp culling: a warp owns an 8x4 pixel block of the tile. The thread that
+// stages a list entry also works out, once for the whole CTA, which of the
+// tile's eight blocks the entry can reach: for each block row (a slab of four
+// pixel rows) it takes the x extent of the entry's alpha >= 1/255 ellipse
+// within the slab (closed form, two square roots), enlarged for rounding, and
+// compares it with the two block columns. A warp then walks only the entries
+// whose bit for its block is set (one ballot per 32 entries). A culled pair
+// lies outside that ellipse, where the exact alpha is below 1/255 and the
+// reference skips it too. Forward and adjoint stage entries with the same
+// function, so they cull the same pairs.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 
@@ -46,43 +48,91 @@ constexpr float kLn2 = 0.6931471805599453f;
 //   alpha = min(0.99, o * 2^p2) < 1/255  <=>  p2 < thr = log2(1 / (255 o))
 // is decided before the exponential. Forward and adjoint stage and test
 // entries with the same functions, so they take identical decisions.
-struct Staged {
-    float2 xy;   // px, py
-    float4 q;    // qa = -0.5 log2e cx, qb = -log2e cy, qc = -0.5 log2e cz, thr
-    float4 col;  // r, g, b, opacity
-    float4 box;  // x_min, x_max, y_min, y_max of the alpha >= 1/255 ellipse (empty: min > max)
-};
+//   xy    px, py
+//   q     qa = -0.5 log2e cx, qb = -log2e cy, qc = -0.5 log2e cz, thr
+//   col   r, g, b, opacity
+//   mask  bit w: the entry can reach alpha >= 1/255 in warp w's 8x4 block
 
 constexpr float kInf = __builtin_huge_valf();
 
-// Box of {d : cx dx^2 + 2 cy dx dy + cz dy^2 <= r2}, r2 = -2 ln2 thr (p2 >= thr
-// there): half-widths sqrt(r2 cz / det), sqrt(r2 cx / det), det = cx cz - cy^2
-// as a compensated difference of products (Kahan), widened for rounding.
-__device__ __forceinline__ float4 alpha_box(float x, float y, float cx, float cy, float cz, float thr) {
-    if (!(thr <= 0.0f)) return make_float4(kInf, -kInf, kInf, -kInf);  // alpha < 1/255 everywhere
-    const float w = cy * cy;
-    const float det = __fmaf_rn(cx, cz, -w) + __fmaf_rn(-cy, cy, w);
-    if (!(det > 0.0f)) return make_float4(-kInf, kInf, -kInf, kInf);  // not an ellipse: never culled
-    const float r2 = -2.0f * kLn2 * thr * (1.0f + 2e-3f);
-    const float hx = sqrtf(r2 * cz / det) + 0.01f, hy = sqrtf(r2 * cx / det) + 0.01f;
-    return make_float4(x - hx, x + hx, y - hy, y + hy);
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
-__device__ __forceinline__ void stage_entry(const Splat* sp, float2& xy, float4& q, float4& col, float4& box) {
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Blocks of the tile at pixel origin (ox, oy) that the entry can reach: bit
+// 2k + c for block row k (pixel rows oy + 4k .. oy + 4k + 3) and block column
+// c (pixel columns ox + 8c .. ox + 8c + 7), the block of warp 2k + c.
+//
+// With a = -qa, b = -qb / 2, c = -qc and d = centre - pixel, a pixel is kept
+// only when p2 >= thr, i.e. inside the ellipse a dx^2 + 2b dx dy + c dy^2 <= R
+// for R = -thr. R is enlarged by 4e-3 (relative and absolute) plus 1e-5 ac/det
+// relative, which bounds the rounding of the per-pixel p2 even for thin
+// ellipses (its terms are at most 4 R ac / det in size there). For dy in a
+// slab, the ellipse spans dx in [(-b dy - s) / a, (-b dy + s) / a],
+// s = sqrt(a R - det dy^2); over the slab the extremes are +-hx (hx =
+// sqrt(c R / det)) when the slab holds the extreme point's dy (-+b hx / c),
+// else the values at the slab's ends. The x extent is widened by 0.02 px +
+// 1e-4 hx for the rounding of this computation. thr > 0 (opacity below
+// 1/255) never blends: no block; a conic that is not positive definite is
+// never culled: every block.
+__device__ __forceinline__ uint32_t block_mask(float cx, float cy, float4 q, float ox, float oy) {
+    const float thr = q.w;
+    if (!(thr <= 0.0f)) return 0u;
+    const float a = -q.x, c = -q.z, b = -0.5f * q.y;
+    const float w = b * b;
+    const float det = __fmaf_rn(a, c, -w) + __fmaf_rn(-b, b, w);  // compensated a c - b^2
+    if (!(a > 0.0f && c > 0.0f && det > 0.0f)) return 0xFFu;
+    const float inv_det = rcp_approx(det), inv_a = rcp_approx(a);
+    const float R = -thr * (1.0f + 4e-3f + 1e-5f * (a * c * inv_det)) + 4e-3f;
+    const float hx = sqrt_approx(c * R * inv_det), hy = sqrt_approx(a * R * inv_det);
+    const float dyr = -b * hx * rcp_approx(c);  // dy of the rightmost point; the leftmost at -dyr
+    const float aR = a * R;
+    const float wx = 0.02f + 1e-4f * hx;
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float y0 = oy + 4.0f * float(k);
+        float dlo = cy - (y0 + 3.0f) - 0.01f, dhi = cy - y0 + 0.01f;
+        if (dhi < -hy || dlo > hy) continue;
+        dlo = fmaxf(dlo, -hy);
+        dhi = fminf(dhi, hy);
+        const float s0 = sqrt_approx(fmaxf(__fmaf_rn(-det, dlo * dlo, aR), 0.0f));
+        const float s1 = sqrt_approx(fmaxf(__fmaf_rn(-det, dhi * dhi, aR), 0.0f));
+        float xmax = fmaxf((-b * dlo + s0) * inv_a, (-b * dhi + s1) * inv_a);
+        float xmin = fminf((-b * dlo - s0) * inv_a, (-b * dhi - s1) * inv_a);
+        if (dyr >= dlo && dyr <= dhi) xmax = hx;
+        if (-dyr >= dlo && -dyr <= dhi) xmin = -hx;
+        const float pxlo = cx - xmax - wx, pxhi = cx - xmin + wx;  // pixel x = centre x - dx
+        if (pxlo <= ox + 7.0f && pxhi >= ox) m |= 1u << (2 * k);
+        if (pxlo <= ox + 15.0f && pxhi >= ox + 8.0f) m |= 2u << (2 * k);
+    }
+    return m;
+}
+
+__device__ __forceinline__ void stage_entry(const Splat* sp, float ox, float oy, float2& xy, float4& q, float4& col,
+                                            uint8_t& mask) {
     const float4* p = reinterpret_cast<const float4*>(sp);
     const float4 c = __ldg(p + 0), tex = __ldg(p + 1), co = __ldg(p + 2);
     xy = make_float2(tex.x, tex.y);
     const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : kInf;  // +inf: never blends
     q = make_float4(-0.5f * kLog2e * co.x, -kLog2e * co.y, -0.5f * kLog2e * co.z, thr);
     col = make_float4(c.x, c.y, c.z, co.w);
-    box = alpha_box(tex.x, tex.y, co.x, co.y, co.z, thr);
+    mask = uint8_t(block_mask(tex.x, tex.y, q, ox, oy));
 }
 
-__device__ __forceinline__ void stage_empty(float2& xy, float4& q, float4& col, float4& box) {
+__device__ __forceinline__ void stage_empty(float2& xy, float4& q, float4& col, uint8_t& mask) {
     xy = make_float2(0.f, 0.f);
     q = make_float4(0.f, 0.f, 0.f, kInf);
     col = make_float4(0.f, 0.f, 0.f, 0.f);
-    box = make_float4(kInf, -kInf, kInf, -kInf);
+    mask = 0u;
 }
 
 // Pixel of thread tid within its tile, and the 8x4 block of its warp.
@@ -92,38 +142,6 @@ __device__ __forceinline__ void warp_block_pixel(uint32_t tid, uint32_t& lx, uin
     by = 4u * (warp >> 1);
     lx = bx + (lane & 7u);
     ly = by + (lane >> 3);
-}
-
-// true when entry box b meets the pixel block [x0, x0+7] x [y0, y0+3]
-__device__ __forceinline__ bool box_meets(float4 b, float x0, float y0) {
-    return b.x <= x0 + 7.0f && b.y >= x0 && b.z <= y0 + 3.0f && b.w >= y0;
-}
-
-// Largest p2 on the rectangle's edge with d = (dx, fixed dy) or (fixed dx, dy).
-__device__ __forceinline__ float edge_p2(float4 q, float dx, float dy) {
-    const float f = q.x * dx * dx + q.y * dx * dy + q.z * dy * dy;
-    // a bound on the rounding of f in single precision, so the test stays conservative
-    const float mag = fabsf(q.x) * dx * dx + fabsf(q.y * dx * dy) + fabsf(q.z) * dy * dy;
-    return f + 1e-5f * mag;
-}
-
-// true when the entry can reach alpha >= 1/255 somewhere in the pixel block
-// [x0, x0+7] x [y0, y0+3]: p2 is a concave quadratic in (dx, dy), so its
-// maximum over the block is 0 at the centre when the centre lies inside,
-// else on an edge, at the edge's vertex clamped to the edge. The threshold is
-// lowered by 1e-3 |thr| + 1e-3 so rounding can only keep an entry, never cull
-// one the exact test keeps.
-__device__ __forceinline__ bool entry_meets_block(float2 c, float4 q, float4 b, float x0, float y0) {
-    if (!box_meets(b, x0, y0)) return false;
-    const float lox = x0 - c.x, hix = lox + 7.0f, loy = y0 - c.y, hiy = loy + 3.0f;
-    if (lox <= 0.0f && hix >= 0.0f && loy <= 0.0f && hiy >= 0.0f) return true;
-    const float ry = __fdividef(-0.5f * q.y, q.z);  // vertex of a vertical edge: dy = ry dx
-    const float rx = __fdividef(-0.5f * q.y, q.x);  // of a horizontal edge: dx = rx dy
-    float best = edge_p2(q, lox, fminf(fmaxf(ry * lox, loy), hiy));
-    best = fmaxf(best, edge_p2(q, hix, fminf(fmaxf(ry * hix, loy), hiy)));
-    best = fmaxf(best, edge_p2(q, fminf(fmaxf(rx * loy, lox), hix), loy));
-    best = fmaxf(best, edge_p2(q, fminf(fmaxf(rx * hiy, lox), hix), hiy));
-    return best >= q.w - (1e-3f * fabsf(q.w) + 1e-3f);
 }
 
 __device__ __forceinline__ float pair_p2(float2 xy, float4 q, float pxf, float pyf, float& dx, float& dy) {
@@ -160,17 +178,17 @@ struct BlendStage {
     float2 xy[2][kBlendThreads];
     float4 q[2][kBlendThreads];
     float4 col[2][kBlendThreads];
-    float4 box[2][kBlendThreads];
+    uint8_t mask[2][kBlendThreads];
 };
 
 __device__ __forceinline__ void stage_slot(BlendStage& S, uint32_t b, uint32_t tid, uint32_t j, const BlendArgs& a,
-                                           const Splat* vsplats) {
+                                           const Splat* vsplats, float ox, float oy) {
     if (!TPD_INBOUNDS(a.ctl, 40, j, a.capacity)) return;
     const uint32_t idx = a.vals[j];
     if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n))
-        stage_entry(vsplats + idx, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);
+        stage_entry(vsplats + idx, ox, oy, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);
     else
-        stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);  // only reachable with corrupted lists
+        stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);  // only reachable with corrupted lists
 }
 
 // Rounds of 256 list entries, double-buffered: while the warps walk round r,
@@ -188,7 +206,8 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     uint32_t lx, ly, bx, by;
     warp_block_pixel(tid, lx, ly, bx, by);
     const uint32_t pxl = tx * kBlockX + lx, pyl = ty * kBlockY + ly;
-    const float bxf = float(tx * kBlockX + bx), byf = float(ty * kBlockY + by);
+    const float ox = float(tx * kBlockX), oy = float(ty * kBlockY);
+    const uint32_t warp = tid >> 5;
     const bool inside = pxl < W && pyl < H;
     const float pxf = float(pxl), pyf = float(pyl);
     const uint32_t K = min(a.ctl->total_keys, a.capacity);
@@ -202,20 +221,19 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     bool done = !inside;
     float T = 1.0f, C0 = 0.f, C1 = 0.f, C2 = 0.f;
     uint32_t last = 0;
-    if (start < end && start + tid < end) stage_slot(S, 0, tid, start + tid, a, vsplats);
+    if (start < end && start + tid < end) stage_slot(S, 0, tid, start + tid, a, vsplats, ox, oy);
     bool all_done = __syncthreads_count(done) == kBlendThreads;
     uint32_t r = 0;
     for (uint32_t b0 = start; b0 < end && !all_done; b0 += kBlendThreads, ++r) {
         const uint32_t b = r & 1u;
         // the next round's entry, into the buffer the last barrier released
-        if (b0 + kBlendThreads + tid < end) stage_slot(S, b ^ 1u, tid, b0 + kBlendThreads + tid, a, vsplats);
+        if (b0 + kBlendThreads + tid < end) stage_slot(S, b ^ 1u, tid, b0 + kBlendThreads + tid, a, vsplats, ox, oy);
         const uint32_t n = min(kBlendThreads, end - b0);
         if (!TPD_INBOUNDS(a.ctl, 43, n, kBlendThreads + 1)) break;
         for (uint32_t g = 0; g < n; g += 32) {
             if (__all_sync(0xFFFFFFFFu, done)) break;
             const uint32_t e = g + lane;
-            uint32_t m = __ballot_sync(0xFFFFFFFFu,
-                                       e < n && entry_meets_block(S.xy[b][e], S.q[b][e], S.box[b][e], bxf, byf));
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, e < n && ((S.mask[b][e] >> warp) & 1u));
             // branch-free body: every lane evaluates the pair and selects the
             // update, so a warp whose lanes take different decisions does not
             // run the paths one after another
@@ -330,7 +348,8 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
     uint32_t lx, ly, bx, by;
     warp_block_pixel(tid, lx, ly, bx, by);
     const uint32_t pxl = tx * kBlockX + lx, pyl = ty * kBlockY + ly;
-    const float bxf = float(tx * kBlockX + bx), byf = float(ty * kBlockY + by);
+    const float ox = float(tx * kBlockX), oy = float(ty * kBlockY);
+    const uint32_t warp = tid >> 5;
     const bool inside = pxl < W && pyl < H;
     const float pxf = float(pxl), pyf = float(pyl);
     const uint32_t K = min(a.ctl->total_keys, a.capacity);
@@ -369,10 +388,10 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
             const uint32_t e = uint32_t(r_end) - 1u - tid;
             uint32_t idx = a.vals[start + e];
             if (idx < a.n) {
-                stage_entry(vsplats + idx, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);
+                stage_entry(vsplats + idx, ox, oy, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);
             } else {  // only reachable with corrupted lists
                 idx = 0;
-                stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.box[b][tid]);
+                stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);
             }
             s_idx[bi][tid] = idx;
         }
@@ -389,8 +408,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
         const uint32_t skip = uint32_t(r_end) > warp_last ? uint32_t(r_end) - warp_last : 0u;
         for (uint32_t g = skip & ~31u; g < n; g += 32) {
             const uint32_t jl = g + lane;
-            uint32_t m = __ballot_sync(0xFFFFFFFFu, jl < n && jl >= skip &&
-                                                        entry_meets_block(S.xy[b][jl], S.q[b][jl], S.box[b][jl], bxf, byf));
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, jl < n && jl >= skip && ((S.mask[b][jl] >> warp) & 1u));
             while (m) {
                 const uint32_t jj = g + uint32_t(__ffs(m) - 1);
                 m &= m - 1u;
