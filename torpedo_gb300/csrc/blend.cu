@@ -6,29 +6,33 @@
 // gathered per contributing pair) dispatched by GaussianEngine.cpp:857-862.
 // The reference has no backward pass; blend_backward_kernel is new.
 //
-// GB300 form: a CTA of 256 threads per tile; each round stages position,
-// conic+opacity and colour of 256 list entries into shared memory (colour is
-// staged with the rest instead of gathered per pair), the whole CTA leaves as
-// soon as every pixel is done (__syncthreads_count), and per pixel the final
+// GB300 form: one CTA per tile; each round stages position, conic+opacity
+// and colour of the next list entries into shared memory (colour is staged
+// with the rest instead of gathered per pair), the whole CTA leaves as soon
+// as every pixel is done (__syncthreads_count), and per pixel the final
 // transmittance and the number of list entries up to the last contributor
-// are kept for the adjoint. The adjoint walks each tile's list back to front,
-// recomputing transmittance as T / (1 - alpha) from the final T (no per-pixel
-// lists), and accumulates per-Gaussian gradients warp-reduced, then in
-// shared memory, then with one global atomic per (round, Gaussian, field).
+// are kept for the adjoint. The forward runs 128 threads with two pixels per
+// lane, whose pair arithmetic uses packed f32x2 operations. The adjoint (256
+// threads, one pixel each) walks each tile's list back to front, recomputing
+// transmittance as T / (1 - alpha) from the final T (no per-pixel lists), and
+// accumulates per-Gaussian gradients warp-reduced, then in shared memory,
+// then with one global atomic per (round, Gaussian, field).
 //
-// power/alpha are computed by one inline function with explicit rounding
-// intrinsics, so the forward and the adjoint take identical decisions.
+// Every per-pixel operation (p2, alpha, the skip and stop tests) has the same
+// operations and explicit rounding in the forward and in the adjoint, so both
+// take identical decisions.
 //
-// Warp culling: a warp owns an 8x4 pixel block of the tile. The thread that
-// stages a list entry also works out, once for the whole CTA, which of the
-// tile's eight blocks the entry can reach: for each block row (a slab of four
-// pixel rows) it takes the x extent of the entry's alpha >= 1/255 ellipse
-// within the slab (closed form, two square roots), enlarged for rounding, and
-// compares it with the two block columns. A warp then walks only the entries
-// whose bit for its block is set (one ballot per 32 entries). A culled pair
-// lies outside that ellipse, where the exact alpha is below 1/255 and the
-// reference skips it too. Forward and adjoint stage entries with the same
-// function, so they cull the same pairs.
+// Warp culling: a warp owns a pixel block of the tile (8x8 in the forward,
+// 8x4 in the adjoint). The thread that stages a list entry also works out,
+// once for the whole CTA, which of the tile's blocks the entry can reach: for
+// each block row (a slab of pixel rows) it takes the x extent of the entry's
+// alpha >= 1/255 ellipse within the slab (closed form, two square roots),
+// enlarged for rounding, and compares it with the two block columns. A warp
+// then walks only the entries whose bit for its block is set (one ballot per
+// 32 entries). A culled pair lies outside that ellipse, where the pair's own
+// test finds alpha below 1/255 and skips it, as the reference does; so the
+// culling changes which skipped pairs are visited, never a result, and the
+// forward and the adjoint may use different blocks.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 
@@ -67,9 +71,10 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return y;
 }
 
-// Blocks of the tile at pixel origin (ox, oy) that the entry can reach: bit
-// 2k + c for block row k (pixel rows oy + 4k .. oy + 4k + 3) and block column
-// c (pixel columns ox + 8c .. ox + 8c + 7), the block of warp 2k + c.
+// Blocks of the tile at pixel origin (ox, oy) that the entry can reach, for
+// blocks 8 pixels wide and 16 / kSlabs high: bit 2k + c for block row k
+// (pixel rows oy + hk .. oy + hk + h - 1, h = 16 / kSlabs) and block column c
+// (pixel columns ox + 8c .. ox + 8c + 7), the block of warp 2k + c.
 //
 // With a = -qa, b = -qb / 2, c = -qc and d = centre - pixel, a pixel is kept
 // only when p2 >= thr, i.e. inside the ellipse a dx^2 + 2b dx dy + c dy^2 <= R
@@ -83,7 +88,9 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // 1e-4 hx for the rounding of this computation. thr > 0 (opacity below
 // 1/255) never blends: no block; a conic that is not positive definite is
 // never culled: every block.
+template <int kSlabs>
 __device__ __forceinline__ uint32_t block_mask(float cx, float cy, float4 q, float ox, float oy) {
+    constexpr float kSlabRows = float(kBlockY / kSlabs);  // pixel rows per block row
     const float thr = q.w;
     if (!(thr <= 0.0f)) return 0u;
     const float a = -q.x, c = -q.z, b = -0.5f * q.y;
@@ -98,9 +105,9 @@ __device__ __forceinline__ uint32_t block_mask(float cx, float cy, float4 q, flo
     const float wx = 0.02f + 1e-4f * hx;
     uint32_t m = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float y0 = oy + 4.0f * float(k);
-        float dlo = cy - (y0 + 3.0f) - 0.01f, dhi = cy - y0 + 0.01f;
+    for (int k = 0; k < kSlabs; ++k) {
+        const float y0 = oy + kSlabRows * float(k);
+        float dlo = cy - (y0 + (kSlabRows - 1.0f)) - 0.01f, dhi = cy - y0 + 0.01f;
         if (dhi < -hy || dlo > hy) continue;
         dlo = fmaxf(dlo, -hy);
         dhi = fminf(dhi, hy);
@@ -125,7 +132,7 @@ __device__ __forceinline__ void stage_entry(const Splat* sp, float ox, float oy,
     const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : kInf;  // +inf: never blends
     q = make_float4(-0.5f * kLog2e * co.x, -kLog2e * co.y, -0.5f * kLog2e * co.z, thr);
     col = make_float4(c.x, c.y, c.z, co.w);
-    mask = uint8_t(block_mask(tex.x, tex.y, q, ox, oy));
+    mask = uint8_t(block_mask<4>(tex.x, tex.y, q, ox, oy));
 }
 
 __device__ __forceinline__ void stage_empty(float2& xy, float4& q, float4& col, uint8_t& mask) {
@@ -173,7 +180,7 @@ __device__ __forceinline__ void load_view_tile(const BlendArgs* /*unused*/, cons
     ty = local / gx;
 }
 
-// Stages list entry j (of the tile's [start, end)) into slot tid of buffer b.
+// Staging buffers of the adjoint: list entry tid of a round in slot tid.
 struct BlendStage {
     float2 xy[2][kBlendThreads];
     float4 q[2][kBlendThreads];
@@ -181,35 +188,74 @@ struct BlendStage {
     uint8_t mask[2][kBlendThreads];
 };
 
-__device__ __forceinline__ void stage_slot(BlendStage& S, uint32_t b, uint32_t tid, uint32_t j, const BlendArgs& a,
-                                           const Splat* vsplats, float ox, float oy) {
-    if (!TPD_INBOUNDS(a.ctl, 40, j, a.capacity)) return;
-    const uint32_t idx = a.vals[j];
-    if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n))
-        stage_entry(vsplats + idx, ox, oy, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);
-    else
-        stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);  // only reachable with corrupted lists
+// ---- forward
+//
+// A CTA of 128 threads per tile. Warp w owns the 8x8 block at (8 (w & 1),
+// 8 (w >> 1)) of the tile, and lane l the two pixels (l & 7, l >> 3) and
+// (l & 7, (l >> 3) + 4) of that block. The two pixels of a lane share dx, and
+// the arithmetic of a (pixel, entry) pair runs on both pixels at once with
+// packed f32x2 operations: per pixel the same operations, in the same order
+// and rounding, as the scalar form in pair_p2 and the adjoint. A staged entry
+// holds its values duplicated in register-pair order, so the packed operands
+// come straight out of five broadcast shared-memory loads.
+constexpr uint32_t kFwdThreads = 128;
+// 128 list entries per staged round (20 KB of shared memory) and at most 64
+// registers: 8 CTAs (32 warps) per SM, measured faster than 256-entry rounds
+// at 5 CTAs, 64-entry rounds, or 10 CTAs at 48 registers
+constexpr uint32_t kRound = 128;
+constexpr uint32_t kFwdMinBlocks = 8;
+
+struct PairStaged {  // 80 bytes
+    float4 xy;       // x, x, y, y
+    float4 qab;      // qa, qa, qb, qb
+    float4 qco;      // qc, qc, opacity, opacity
+    float4 rg;       // r, r, g, g
+    float4 bt;       // b, b, thr, 0
+};
+
+struct FwdStage {
+    PairStaged e[2][kRound];
+    uint8_t mask[2][kRound];  // bit w: the entry can reach warp w's 8x8 block
+};
+
+__device__ __forceinline__ void stage_pair_entry(const Splat* sp, float ox, float oy, PairStaged& d, uint8_t& mask) {
+    const float4* p = reinterpret_cast<const float4*>(sp);
+    const float4 c = __ldg(p + 0), tex = __ldg(p + 1), co = __ldg(p + 2);
+    const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : kInf;  // +inf: never blends
+    const float4 q = make_float4(-0.5f * kLog2e * co.x, -kLog2e * co.y, -0.5f * kLog2e * co.z, thr);
+    d.xy = make_float4(tex.x, tex.x, tex.y, tex.y);
+    d.qab = make_float4(q.x, q.x, q.y, q.y);
+    d.qco = make_float4(q.z, q.z, co.w, co.w);
+    d.rg = make_float4(c.x, c.x, c.y, c.y);
+    d.bt = make_float4(c.z, c.z, thr, 0.0f);
+    mask = uint8_t(block_mask<2>(tex.x, tex.y, q, ox, oy));
 }
 
-// Rounds of 256 list entries, double-buffered: while the warps walk round r,
-// each thread stages its entry of round r + 1 into the other buffer, and one
-// barrier per round (which also counts finished pixels) separates the two.
-__global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
-    __shared__ BlendStage S;
+__device__ __forceinline__ void stage_pair_empty(PairStaged& d, uint8_t& mask) {
+    d.xy = d.qab = d.qco = d.rg = make_float4(0.f, 0.f, 0.f, 0.f);
+    d.bt = make_float4(0.f, 0.f, kInf, 0.f);
+    mask = 0u;
+}
+
+// Rounds of kRound list entries, double-buffered: while the warps walk round
+// r, each thread stages its entry of round r + 1 into the other buffer, and
+// one barrier per round (which also counts finished pixels) separates the
+// two.
+__global__ void __launch_bounds__(kFwdThreads, kFwdMinBlocks) blend_kernel(BlendArgs a) {
+    __shared__ FwdStage S;
 
     const uint32_t tile = blockIdx.x;
     // an overflowed frame is re-rendered with larger key buffers; nothing to draw
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
     uint32_t vi, W, H, tx, ty;
     load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    uint32_t lx, ly, bx, by;
-    warp_block_pixel(tid, lx, ly, bx, by);
-    const uint32_t pxl = tx * kBlockX + lx, pyl = ty * kBlockY + ly;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t px = tx * kBlockX + 8u * (warp & 1u) + (lane & 7u);
+    const uint32_t pya = ty * kBlockY + 8u * (warp >> 1) + (lane >> 3), pyb = pya + 4u;
     const float ox = float(tx * kBlockX), oy = float(ty * kBlockY);
-    const uint32_t warp = tid >> 5;
-    const bool inside = pxl < W && pyl < H;
-    const float pxf = float(pxl), pyf = float(pyl);
+    const bool in_a = px < W && pya < H, in_b = px < W && pyb < H;
+    const float2 npx = make_float2(-float(px), -float(px));
+    const float2 npy = make_float2(-float(pya), -float(pyb));
     const uint32_t K = min(a.ctl->total_keys, a.capacity);
     const uint32_t raw_start = a.ranges[tile * 2 + 0], raw_end = a.ranges[tile * 2 + 1];
     const uint32_t end = min(raw_end, K), start = min(raw_start, end);
@@ -218,56 +264,93 @@ __global__ void __launch_bounds__(kBlendThreads) blend_kernel(BlendArgs a) {
     if (tid == 0 && raw_start > raw_end) a.ranges[tile * 2 + 0] = 0u;
     const Splat* vsplats = a.splats + size_t(vi) * a.n;
 
-    bool done = !inside;
-    float T = 1.0f, C0 = 0.f, C1 = 0.f, C2 = 0.f;
-    uint32_t last = 0;
-    if (start < end && start + tid < end) stage_slot(S, 0, tid, start + tid, a, vsplats, ox, oy);
-    bool all_done = __syncthreads_count(done) == kBlendThreads;
+    // entries j0 + tid, j0 + tid + 128, ... (below j0 + kRound) of the list into buffer buf
+    auto stage = [&](uint32_t buf, uint32_t j0) {
+#pragma unroll
+        for (uint32_t k = tid; k < kRound; k += kFwdThreads) {
+            const uint32_t j = j0 + k;
+            if (j >= end || !TPD_INBOUNDS(a.ctl, 40, j, a.capacity)) continue;
+            const uint32_t idx = a.vals[j];
+            if (idx < a.n && TPD_INBOUNDS(a.ctl, 42, idx, a.n))
+                stage_pair_entry(vsplats + idx, ox, oy, S.e[buf][k], S.mask[buf][k]);
+            else
+                stage_pair_empty(S.e[buf][k], S.mask[buf][k]);  // only reachable with corrupted lists
+        }
+    };
+
+    bool done_a = !in_a, done_b = !in_b;
+    float2 T = make_float2(1.0f, 1.0f), C0 = make_float2(0.f, 0.f), C1 = C0, C2 = C0;
+    uint32_t last_a = 0, last_b = 0;
+    const float2 one = make_float2(1.0f, 1.0f), mone = make_float2(-1.0f, -1.0f);
+    if (start < end) stage(0, start);
+    bool all_done = __syncthreads_count(done_a && done_b) == kFwdThreads;
     uint32_t r = 0;
-    for (uint32_t b0 = start; b0 < end && !all_done; b0 += kBlendThreads, ++r) {
+    for (uint32_t b0 = start; b0 < end && !all_done; b0 += kRound, ++r) {
         const uint32_t b = r & 1u;
-        // the next round's entry, into the buffer the last barrier released
-        if (b0 + kBlendThreads + tid < end) stage_slot(S, b ^ 1u, tid, b0 + kBlendThreads + tid, a, vsplats, ox, oy);
-        const uint32_t n = min(kBlendThreads, end - b0);
-        if (!TPD_INBOUNDS(a.ctl, 43, n, kBlendThreads + 1)) break;
+        // the next round's entries, into the buffer the last barrier released
+        if (b0 + kRound < end) stage(b ^ 1u, b0 + kRound);
+        const uint32_t n = min(kRound, end - b0);
+        const uint32_t lbase = b0 - start + 1u;  // n_contrib of entry jj of this round: lbase + jj
         for (uint32_t g = 0; g < n; g += 32) {
-            if (__all_sync(0xFFFFFFFFu, done)) break;
+            if (__all_sync(0xFFFFFFFFu, done_a && done_b)) break;
             const uint32_t e = g + lane;
             uint32_t m = __ballot_sync(0xFFFFFFFFu, e < n && ((S.mask[b][e] >> warp) & 1u));
-            // branch-free body: every lane evaluates the pair and selects the
-            // update, so a warp whose lanes take different decisions does not
-            // run the paths one after another
+            // branch-free body: every lane evaluates both pairs and selects
+            // the update, so lanes taking different decisions do not run the
+            // paths one after another. A skipped pair gets alpha = 0, which
+            // leaves T and C exactly as they were.
             while (m) {
                 const uint32_t jj = g + uint32_t(__ffs(m) - 1);
                 m &= m - 1u;
-                float dx, dy;
-                const float4 q = S.q[b][jj];
-                const float p2 = pair_p2(S.xy[b][jj], q, pxf, pyf, dx, dy);
-                const float4 col = S.col[b][jj];
-                const float alpha = fminf(kAlphaMax, __fmul_rn(col.w, ex2_approx(p2)));
-                const float tn = __fmul_rn(T, __fsub_rn(1.0f, alpha));
-                const bool live = !done && !pair_skipped(p2, q.w);
-                const bool term = live && tn < kTMin;
-                const bool add = live && !term;
-                done = done || term;
-                // a pair that does not contribute adds col * 0: C stays the same for finite colours
-                const float w = add ? __fmul_rn(alpha, T) : 0.0f;
-                C0 = __fmaf_rn(col.x, w, C0);
-                C1 = __fmaf_rn(col.y, w, C1);
-                C2 = __fmaf_rn(col.z, w, C2);
-                T = add ? tn : T;
-                last = add ? b0 + jj - start + 1 : last;
+                const PairStaged& E = S.e[b][jj];
+                const float4 xy = E.xy, qab = E.qab, qco = E.qco, rg = E.rg, bt = E.bt;
+                // pair_p2 for both pixels: dx = x - px, dy = y - py,
+                // p2 = fma(fma(qb, dy, qa dx), dx, (qc dy) dy)
+                const float2 dx = __fadd2_rn(make_float2(xy.x, xy.y), npx);
+                const float2 dy = __fadd2_rn(make_float2(xy.z, xy.w), npy);
+                const float2 t = __ffma2_rn(make_float2(qab.z, qab.w), dy, __fmul2_rn(make_float2(qab.x, qab.y), dx));
+                const float2 p2 = __ffma2_rn(t, dx, __fmul2_rn(__fmul2_rn(make_float2(qco.x, qco.y), dy), dy));
+                const float2 ao =
+                    __fmul2_rn(make_float2(qco.z, qco.w), make_float2(ex2_approx(p2.x), ex2_approx(p2.y)));
+                const bool skip_a = done_a || pair_skipped(p2.x, bt.z);
+                const bool skip_b = done_b || pair_skipped(p2.y, bt.z);
+                const float2 alpha = make_float2(skip_a ? 0.0f : fminf(kAlphaMax, ao.x),
+                                                 skip_b ? 0.0f : fminf(kAlphaMax, ao.y));
+                const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
+                const bool term_a = tn.x < kTMin, term_b = tn.y < kTMin;  // false when skipped: tn = T
+                const bool add_a = !skip_a && !term_a, add_b = !skip_b && !term_b;
+                done_a = done_a || term_a;
+                done_b = done_b || term_b;
+                const float2 aT = __fmul2_rn(alpha, T);
+                const float2 w = make_float2(term_a ? 0.0f : aT.x, term_b ? 0.0f : aT.y);
+                C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
+                C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
+                C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
+                T = make_float2(term_a ? T.x : tn.x, term_b ? T.y : tn.y);
+                last_a = add_a ? lbase + jj : last_a;
+                last_b = add_b ? lbase + jj : last_b;
             }
         }
-        all_done = __syncthreads_count(done) == kBlendThreads;
+        all_done = __syncthreads_count(done_a && done_b) == kFwdThreads;
     }
-    if (inside && TPD_INBOUNDS(a.ctl, 41, tile, a.n_tiles)) {
-        const size_t p = (a.image_offset ? a.image_offset[vi] : 0ull) + size_t(pyl) * W + pxl;
-        a.image[p * 3 + 0] = C0;
-        a.image[p * 3 + 1] = C1;
-        a.image[p * 3 + 2] = C2;
-        if (a.final_T) a.final_T[p] = T;
-        if (a.n_contrib) a.n_contrib[p] = last;
+    if (TPD_INBOUNDS(a.ctl, 41, tile, a.n_tiles)) {
+        const size_t img0 = a.image_offset ? a.image_offset[vi] : 0ull;
+        if (in_a) {
+            const size_t p = img0 + size_t(pya) * W + px;
+            a.image[p * 3 + 0] = C0.x;
+            a.image[p * 3 + 1] = C1.x;
+            a.image[p * 3 + 2] = C2.x;
+            if (a.final_T) a.final_T[p] = T.x;
+            if (a.n_contrib) a.n_contrib[p] = last_a;
+        }
+        if (in_b) {
+            const size_t p = img0 + size_t(pyb) * W + px;
+            a.image[p * 3 + 0] = C0.y;
+            a.image[p * 3 + 1] = C1.y;
+            a.image[p * 3 + 2] = C2.y;
+            if (a.final_T) a.final_T[p] = T.y;
+            if (a.n_contrib) a.n_contrib[p] = last_b;
+        }
     }
 }
 
@@ -477,7 +560,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBack
 
 void launch_blend(const BlendArgs& a, cudaStream_t s) {
     if (a.n_tiles == 0) return;
-    blend_kernel<<<a.n_tiles, kBlendThreads, 0, s>>>(a);
+    blend_kernel<<<a.n_tiles, kFwdThreads, 0, s>>>(a);
 }
 
 void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStream_t s) {
