@@ -6,56 +6,52 @@
 // gathered per contributing pair) dispatched by GaussianEngine.cpp:857-862.
 // The reference has no backward pass; blend_backward_kernel is new.
 //
-// GB300 form: one CTA per tile; each round stages position, conic+opacity
-// and colour of the next list entries into shared memory (colour is staged
-// with the rest instead of gathered per pair), the whole CTA leaves as soon
-// as every pixel is done (__syncthreads_count), and per pixel the final
-// transmittance and the number of list entries up to the last contributor
-// are kept for the adjoint. The forward runs 128 threads with two pixels per
-// lane, whose pair arithmetic uses packed f32x2 operations. The adjoint (256
-// threads, one pixel each) walks each tile's list back to front, recomputing
-// transmittance as T / (1 - alpha) from the final T (no per-pixel lists), and
-// accumulates per-Gaussian gradients warp-reduced, then in shared memory,
-// then with one global atomic per (round, Gaussian, field).
+// GB300 form: one CTA of 128 threads per tile, each lane on two pixels whose
+// pair arithmetic runs in packed f32x2 operations; each round stages
+// position, conic+opacity and colour of the next list entries into shared
+// memory (colour is staged with the rest instead of gathered per pair), the
+// whole CTA leaves as soon as every pixel is done (__syncthreads_count), and
+// per pixel the final transmittance and the number of list entries up to the
+// last contributor are kept for the adjoint. The adjoint walks each tile's
+// list back to front, recomputing transmittance as T / (1 - alpha) from the
+// final T (no per-pixel lists), and accumulates per-Gaussian gradients
+// warp-reduced, then in shared memory, then with one global atomic per
+// (round, Gaussian, field).
 //
 // Every per-pixel operation (p2, alpha, the skip and stop tests) has the same
 // operations and explicit rounding in the forward and in the adjoint, so both
 // take identical decisions.
 //
-// Warp culling: a warp owns a pixel block of the tile (8x8 in the forward,
-// 8x4 in the adjoint). The thread that stages a list entry also works out,
-// once for the whole CTA, which of the tile's blocks the entry can reach: for
-// each block row (a slab of pixel rows) it takes the x extent of the entry's
-// alpha >= 1/255 ellipse within the slab (closed form, two square roots),
-// enlarged for rounding, and compares it with the two block columns. A warp
-// then walks only the entries whose bit for its block is set (one ballot per
-// 32 entries). A culled pair lies outside that ellipse, where the pair's own
-// test finds alpha below 1/255 and skips it, as the reference does; so the
-// culling changes which skipped pairs are visited, never a result, and the
-// forward and the adjoint may use different blocks.
+// Warp culling: a warp owns an 8x8 pixel block of the tile. The thread that
+// stages a list entry also works out, once for the whole CTA, which of the
+// tile's four blocks the entry can reach: for each block row (a slab of
+// pixel rows) it takes the x extent of the entry's alpha >= 1/255 ellipse
+// within the slab (closed form, two square roots), enlarged for rounding,
+// and compares it with the two block columns. A warp then walks only the
+// entries whose bit for its block is set (one ballot per 32 entries). A
+// culled pair lies outside that ellipse, where the pair's own test finds
+// alpha below 1/255 and skips it, as the reference does; so the culling
+// changes which skipped pairs are visited, never a result.
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 
 namespace tpd {
 namespace {
 
-constexpr uint32_t kBlendThreads = kTilePixels;  // 256
 constexpr float kAlphaMax = 0.99f;
 constexpr float kTMin = 0.0001f;
 
 constexpr float kLog2e = 1.4426950408889634f;
 constexpr float kLn2 = 0.6931471805599453f;
 
-// A list entry staged in shared memory. The conic is pre-scaled so that
-//   p2 = log2(e) * power,  power = -0.5 * (cx*dx*dx + cz*dy*dy) - cy*dx*dy  (blend.slang:83-84)
-// costs five multiply/fma operations, exp(power) = 2^p2 is one ex2, and
+// Per (pixel, entry) pair, with the conic pre-scaled at staging
+//   qa = -0.5 log2e cx, qb = -log2e cy, qc = -0.5 log2e cz,
+//   dx = x - px, dy = y - py (rounded subtractions),
+//   p2 = fma(fma(qb, dy, qa dx), dx, (qc dy) dy) = log2(e) * power,
+//   power = -0.5 * (cx*dx*dx + cz*dy*dy) - cy*dx*dy  (blend.slang:83-84),
+// five multiply/fma operations; exp(power) = 2^p2 is one ex2, and
 //   alpha = min(0.99, o * 2^p2) < 1/255  <=>  p2 < thr = log2(1 / (255 o))
-// is decided before the exponential. Forward and adjoint stage and test
-// entries with the same functions, so they take identical decisions.
-//   xy    px, py
-//   q     qa = -0.5 log2e cx, qb = -log2e cy, qc = -0.5 log2e cz, thr
-//   col   r, g, b, opacity
-//   mask  bit w: the entry can reach alpha >= 1/255 in warp w's 8x4 block
+// is decided before the exponential.
 
 constexpr float kInf = __builtin_huge_valf();
 
@@ -124,40 +120,6 @@ __device__ __forceinline__ uint32_t block_mask(float cx, float cy, float4 q, flo
     return m;
 }
 
-__device__ __forceinline__ void stage_entry(const Splat* sp, float ox, float oy, float2& xy, float4& q, float4& col,
-                                            uint8_t& mask) {
-    const float4* p = reinterpret_cast<const float4*>(sp);
-    const float4 c = __ldg(p + 0), tex = __ldg(p + 1), co = __ldg(p + 2);
-    xy = make_float2(tex.x, tex.y);
-    const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : kInf;  // +inf: never blends
-    q = make_float4(-0.5f * kLog2e * co.x, -kLog2e * co.y, -0.5f * kLog2e * co.z, thr);
-    col = make_float4(c.x, c.y, c.z, co.w);
-    mask = uint8_t(block_mask<4>(tex.x, tex.y, q, ox, oy));
-}
-
-__device__ __forceinline__ void stage_empty(float2& xy, float4& q, float4& col, uint8_t& mask) {
-    xy = make_float2(0.f, 0.f);
-    q = make_float4(0.f, 0.f, 0.f, kInf);
-    col = make_float4(0.f, 0.f, 0.f, 0.f);
-    mask = 0u;
-}
-
-// Pixel of thread tid within its tile, and the 8x4 block of its warp.
-__device__ __forceinline__ void warp_block_pixel(uint32_t tid, uint32_t& lx, uint32_t& ly, uint32_t& bx, uint32_t& by) {
-    const uint32_t warp = tid >> 5, lane = tid & 31u;
-    bx = 8u * (warp & 1u);
-    by = 4u * (warp >> 1);
-    lx = bx + (lane & 7u);
-    ly = by + (lane >> 3);
-}
-
-__device__ __forceinline__ float pair_p2(float2 xy, float4 q, float pxf, float pyf, float& dx, float& dy) {
-    dx = __fsub_rn(xy.x, pxf);
-    dy = __fsub_rn(xy.y, pyf);
-    const float t = __fmaf_rn(q.y, dy, __fmul_rn(q.x, dx));
-    return __fmaf_rn(t, dx, __fmul_rn(__fmul_rn(q.z, dy), dy));
-}
-
 __device__ __forceinline__ float ex2_approx(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -180,22 +142,14 @@ __device__ __forceinline__ void load_view_tile(const BlendArgs* /*unused*/, cons
     ty = local / gx;
 }
 
-// Staging buffers of the adjoint: list entry tid of a round in slot tid.
-struct BlendStage {
-    float2 xy[2][kBlendThreads];
-    float4 q[2][kBlendThreads];
-    float4 col[2][kBlendThreads];
-    uint8_t mask[2][kBlendThreads];
-};
-
 // ---- forward
 //
 // A CTA of 128 threads per tile. Warp w owns the 8x8 block at (8 (w & 1),
 // 8 (w >> 1)) of the tile, and lane l the two pixels (l & 7, l >> 3) and
 // (l & 7, (l >> 3) + 4) of that block. The two pixels of a lane share dx, and
 // the arithmetic of a (pixel, entry) pair runs on both pixels at once with
-// packed f32x2 operations: per pixel the same operations, in the same order
-// and rounding, as the scalar form in pair_p2 and the adjoint. A staged entry
+// packed f32x2 operations: per pixel the operations, order and rounding
+// given above for p2, alpha and the tests, as in the adjoint. A staged entry
 // holds its values duplicated in register-pair order, so the packed operands
 // come straight out of five broadcast shared-memory loads.
 constexpr uint32_t kFwdThreads = 128;
@@ -304,8 +258,7 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdMinBlocks) blend_kernel(Blend
                 m &= m - 1u;
                 const PairStaged& E = S.e[b][jj];
                 const float4 xy = E.xy, qab = E.qab, qco = E.qco, rg = E.rg, bt = E.bt;
-                // pair_p2 for both pixels: dx = x - px, dy = y - py,
-                // p2 = fma(fma(qb, dy, qa dx), dx, (qc dy) dy)
+                // p2 for both pixels
                 const float2 dx = __fadd2_rn(make_float2(xy.x, xy.y), npx);
                 const float2 dy = __fadd2_rn(make_float2(xy.z, xy.w), npy);
                 const float2 t = __ffma2_rn(make_float2(qab.z, qab.w), dy, __fmul2_rn(make_float2(qab.x, qab.y), dx));
@@ -367,12 +320,6 @@ __global__ void pack_rgba8_kernel(const float* rgb, uint32_t* rgba, size_t pixel
     rgba[i] = out;
 }
 
-__device__ __forceinline__ float warp_red(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    return v;
-}
-
 constexpr int kG2D = 9;  // px, py, conic.x, conic.y, conic.z, opacity, r, g, b
 
 // Sums v[0..7] over the warp with a transposed butterfly: each of the first
@@ -403,153 +350,185 @@ __device__ __forceinline__ float warp_sum8_transposed(const float (&v)[8], uint3
     return c;
 }
 
-// Rounds of 256 list entries from the back, as in the forward: staging
-// double-buffered, per-round gradient sums in one of two shared buffers. The
-// barrier at the end of a round completes its sums; each thread then adds its
-// share of them to global memory and zeroes what it added, so the buffer is
-// clean when it comes round again two rounds later. The staged indices that
-// the flush reads live in three buffers (the next round's staging overwrites
-// the one of the round before the last).
+// The adjoint, with the forward's layout: a CTA of 128 threads per tile,
+// warp w on the 8x8 block at (8 (w & 1), 8 (w >> 1)), lane l on pixels
+// (l & 7, l >> 3) and (l & 7, (l >> 3) + 4), pair arithmetic packed in f32x2.
+// Rounds of kBwdRound list entries from the back: staging double-buffered,
+// per-round gradient sums in one of two shared buffers. The barrier at the
+// end of a round completes its sums; each thread then adds its share of them
+// to global memory and zeroes what it added, so the buffer is clean when it
+// comes round again two rounds later. The staged indices that the flush
+// reads live in three buffers (the next round's staging overwrites the one of
+// the round before the last).
+//
+// 64 list entries per round (17 KB of shared memory) and at most 64 registers:
+// 8 CTAs per SM; 128-entry rounds at 6 or 7 CTAs per SM measured the same
+constexpr uint32_t kBwdRound = 64;
+constexpr uint32_t kBwdMinBlocks = 8;
 struct BlendBackwardSmem {
-    BlendStage stage;
-    float acc[2][kBlendThreads][kG2DStride];
-    uint32_t idx[3][kBlendThreads];
+    PairStaged e[2][kBwdRound];
+    uint8_t mask[2][kBwdRound];
+    float acc[2][kBwdRound][kG2DStride];
+    uint32_t idx[3][kBwdRound];
+    uint32_t wmax[kFwdThreads / 32];
 };
 
-__global__ void __launch_bounds__(kBlendThreads) blend_backward_kernel(BlendBackwardArgs a) {
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+__global__ void __launch_bounds__(kFwdThreads, kBwdMinBlocks) blend_backward_kernel(BlendBackwardArgs a) {
     extern __shared__ __align__(16) unsigned char bwd_smem[];
     BlendBackwardSmem& SM = *reinterpret_cast<BlendBackwardSmem*>(bwd_smem);
-    BlendStage& S = SM.stage;
-    auto& s_idx = SM.idx;
-    auto& s_acc = SM.acc;
 
     const uint32_t tile = blockIdx.x;
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
     uint32_t vi, W, H, tx, ty;
     load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    uint32_t lx, ly, bx, by;
-    warp_block_pixel(tid, lx, ly, bx, by);
-    const uint32_t pxl = tx * kBlockX + lx, pyl = ty * kBlockY + ly;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t px = tx * kBlockX + 8u * (warp & 1u) + (lane & 7u);
+    const uint32_t pya = ty * kBlockY + 8u * (warp >> 1) + (lane >> 3), pyb = pya + 4u;
     const float ox = float(tx * kBlockX), oy = float(ty * kBlockY);
-    const uint32_t warp = tid >> 5;
-    const bool inside = pxl < W && pyl < H;
-    const float pxf = float(pxl), pyf = float(pyl);
+    const bool in_a = px < W && pya < H, in_b = px < W && pyb < H;
+    const float2 npx = f2(-float(px), -float(px));
+    const float2 npy = f2(-float(pya), -float(pyb));
     const uint32_t K = min(a.ctl->total_keys, a.capacity);
     const uint32_t end = min(a.ranges[tile * 2 + 1], K), start = min(a.ranges[tile * 2 + 0], end);
     const Splat* vsplats = a.splats + size_t(vi) * a.n;
 
-    const size_t p = (a.image_offset ? a.image_offset[vi] : 0ull) + size_t(pyl) * W + pxl;
-    float T = 1.0f, g0 = 0.f, g1 = 0.f, g2 = 0.f;
-    uint32_t last = 0;
-    if (inside) {
-        T = a.final_T[p];
-        last = min(a.n_contrib[p], end - start);
-        g0 = a.dL_dimage[p * 3 + 0];
-        g1 = a.dL_dimage[p * 3 + 1];
-        g2 = a.dL_dimage[p * 3 + 2];
+    const size_t img0 = a.image_offset ? a.image_offset[vi] : 0ull;
+    const size_t pa = img0 + size_t(pya) * W + px, pb = img0 + size_t(pyb) * W + px;
+    float2 T = f2(1.0f, 1.0f), g0 = f2(0.f, 0.f), g1 = g0, g2 = g0;
+    uint32_t last_a = 0, last_b = 0;
+    if (in_a) {
+        T.x = a.final_T[pa];
+        last_a = min(a.n_contrib[pa], end - start);
+        g0.x = a.dL_dimage[pa * 3 + 0];
+        g1.x = a.dL_dimage[pa * 3 + 1];
+        g2.x = a.dL_dimage[pa * 3 + 2];
+    }
+    if (in_b) {
+        T.y = a.final_T[pb];
+        last_b = min(a.n_contrib[pb], end - start);
+        g0.y = a.dL_dimage[pb * 3 + 0];
+        g1.y = a.dL_dimage[pb * 3 + 1];
+        g2.y = a.dL_dimage[pb * 3 + 2];
     }
     // the block walks back from the largest last-contributor index over its
     // pixels; a warp takes entries below its own largest index only
-    uint32_t warp_last = last;
+    uint32_t warp_last = max(last_a, last_b);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) warp_last = max(warp_last, __shfl_xor_sync(0xFFFFFFFFu, warp_last, o));
-    __shared__ uint32_t s_max[kBlendThreads / 32];
-    if (lane == 0) s_max[tid >> 5] = warp_last;
+    if (lane == 0) SM.wmax[warp] = warp_last;
+    for (uint32_t k = tid; k < 2 * kBwdRound * kG2DStride; k += kFwdThreads) (&SM.acc[0][0][0])[k] = 0.f;
     __syncthreads();
     uint32_t max_last = 0;
 #pragma unroll
-    for (uint32_t w = 0; w < kBlendThreads / 32; ++w) max_last = max(max_last, s_max[w]);
+    for (uint32_t w = 0; w < kFwdThreads / 32; ++w) max_last = max(max_last, SM.wmax[w]);
 
-    float S0 = 0.f, S1 = 0.f, S2 = 0.f;  // colour accumulated behind the current entry
+    float2 S0 = f2(0.f, 0.f), S1 = S0, S2 = S0;  // colour accumulated behind the current entry
     float* g2d_view = a.g2d + size_t(vi) * a.g2d_view_stride;
-    // stages the round whose list positions (relative) end at r_end: entry
-    // tid is position r_end - 1 - tid
+    // stages the round whose list positions (relative) end at r_end: slot k
+    // holds position r_end - 1 - k
     auto stage_round = [&](int32_t r_end, uint32_t b, uint32_t bi) {
-        const uint32_t n = uint32_t(min(int32_t(kBlendThreads), r_end));
-        if (tid < n) {
-            const uint32_t e = uint32_t(r_end) - 1u - tid;
+        const uint32_t n = uint32_t(min(int32_t(kBwdRound), r_end));
+        for (uint32_t k = tid; k < n; k += kFwdThreads) {
+            const uint32_t e = uint32_t(r_end) - 1u - k;
             uint32_t idx = a.vals[start + e];
             if (idx < a.n) {
-                stage_entry(vsplats + idx, ox, oy, S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);
+                stage_pair_entry(vsplats + idx, ox, oy, SM.e[b][k], SM.mask[b][k]);
             } else {  // only reachable with corrupted lists
                 idx = 0;
-                stage_empty(S.xy[b][tid], S.q[b][tid], S.col[b][tid], S.mask[b][tid]);
+                stage_pair_empty(SM.e[b][k], SM.mask[b][k]);
             }
-            s_idx[bi][tid] = idx;
+            SM.idx[bi][k] = idx;
         }
     };
-    for (uint32_t k = tid; k < 2 * kBlendThreads * kG2DStride; k += kBlendThreads) (&s_acc[0][0][0])[k] = 0.f;
     if (max_last > 0) stage_round(int32_t(max_last), 0, 0);
     __syncthreads();
+    const float2 one = f2(1.0f, 1.0f), mone = f2(-1.0f, -1.0f), mhalf = f2(-0.5f, -0.5f), ln2 = f2(kLn2, kLn2);
     uint32_t r = 0;
-    for (int32_t r_end = int32_t(max_last); r_end > 0; r_end -= int32_t(kBlendThreads), ++r) {
+    for (int32_t r_end = int32_t(max_last); r_end > 0; r_end -= int32_t(kBwdRound), ++r) {
         const uint32_t b = r & 1u, bi = r % 3u;
-        const uint32_t n = uint32_t(min(int32_t(kBlendThreads), r_end));
-        if (r_end > int32_t(kBlendThreads)) stage_round(r_end - int32_t(kBlendThreads), b ^ 1u, (r + 1) % 3u);
+        const uint32_t n = uint32_t(min(int32_t(kBwdRound), r_end));
+        if (r_end > int32_t(kBwdRound)) stage_round(r_end - int32_t(kBwdRound), b ^ 1u, (r + 1) % 3u);
         // entries jj >= skip have list positions r_end - 1 - jj below warp_last
         const uint32_t skip = uint32_t(r_end) > warp_last ? uint32_t(r_end) - warp_last : 0u;
         for (uint32_t g = skip & ~31u; g < n; g += 32) {
             const uint32_t jl = g + lane;
-            uint32_t m = __ballot_sync(0xFFFFFFFFu, jl < n && jl >= skip && ((S.mask[b][jl] >> warp) & 1u));
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, jl < n && jl >= skip && ((SM.mask[b][jl] >> warp) & 1u));
             while (m) {
                 const uint32_t jj = g + uint32_t(__ffs(m) - 1);
                 m &= m - 1u;
                 const uint32_t e = uint32_t(r_end) - 1u - jj;
-                // branch-free body (as in the forward): every lane evaluates,
-                // the selects keep only contributing pairs
-                float dx, dy;
-                const float4 q = S.q[b][jj];
-                const float p2 = pair_p2(S.xy[b][jj], q, pxf, pyf, dx, dy);
-                const float4 col = S.col[b][jj];
-                const bool contrib = inside && e < last && !pair_skipped(p2, q.w);
-                const float G = ex2_approx(p2);
-                const float raw = __fmul_rn(col.w, G);
-                const float alpha = fminf(kAlphaMax, raw);
-                const float inv = __fdividef(1.0f, 1.0f - alpha);  // 1 - alpha >= 0.01
-                const float Tb = T * inv;  // transmittance in front of this entry
-                // zero weight and gradient scale for pairs that do not count:
-                // every term below is finite, so it adds exactly nothing
-                const float w = contrib ? alpha * Tb : 0.0f;
-                const float dA = g0 * (col.x * Tb - S0 * inv) + g1 * (col.y * Tb - S1 * inv) +
-                                 g2 * (col.z * Tb - S2 * inv);
-                S0 = fmaf(col.x, w, S0);
-                S1 = fmaf(col.y, w, S1);
-                S2 = fmaf(col.z, w, S2);
-                T = contrib ? Tb : T;
+                const PairStaged& E = SM.e[b][jj];
+                const float4 xy = E.xy, qab = E.qab, qco = E.qco, rg = E.rg, bt = E.bt;
+                // p2 for both pixels, as in the forward
+                const float2 dx = __fadd2_rn(f2(xy.x, xy.y), npx);
+                const float2 dy = __fadd2_rn(f2(xy.z, xy.w), npy);
+                const float2 qadx = __fmul2_rn(f2(qab.x, qab.y), dx);
+                const float2 t = __ffma2_rn(f2(qab.z, qab.w), dy, qadx);
+                const float2 qcdy = __fmul2_rn(f2(qco.x, qco.y), dy);
+                const float2 p2 = __ffma2_rn(t, dx, __fmul2_rn(qcdy, dy));
+                const bool ca = in_a && e < last_a && !pair_skipped(p2.x, bt.z);
+                const bool cb = in_b && e < last_b && !pair_skipped(p2.y, bt.z);
+                // branch-free body: zero weight and gradient scale for pairs
+                // that do not count; every term below is finite, so they add
+                // exactly nothing
+                const float2 G = f2(ex2_approx(p2.x), ex2_approx(p2.y));
+                const float2 raw = __fmul2_rn(f2(qco.z, qco.w), G);
+                const float2 alpha = f2(fminf(kAlphaMax, raw.x), fminf(kAlphaMax, raw.y));
+                const float2 om = __ffma2_rn(mone, alpha, one);  // 1 - alpha >= 0.01
+                const float2 inv = f2(__fdividef(1.0f, om.x), __fdividef(1.0f, om.y));
+                const float2 Tb = __fmul2_rn(T, inv);  // transmittance in front of this entry
+                const float2 aTb = __fmul2_rn(alpha, Tb);
+                const float2 w = f2(ca ? aTb.x : 0.0f, cb ? aTb.y : 0.0f);
+                // dL/dalpha = sum_c g_c (col_c Tb - S_c / (1 - alpha))
+                const float2 ninv = __fmul2_rn(inv, mone);
+                const float2 d0 = __ffma2_rn(f2(rg.x, rg.y), Tb, __fmul2_rn(S0, ninv));
+                const float2 d1 = __ffma2_rn(f2(rg.z, rg.w), Tb, __fmul2_rn(S1, ninv));
+                const float2 d2 = __ffma2_rn(f2(bt.x, bt.y), Tb, __fmul2_rn(S2, ninv));
+                const float2 dA = __ffma2_rn(g2, d2, __ffma2_rn(g1, d1, __fmul2_rn(g0, d0)));
+                S0 = __ffma2_rn(f2(rg.x, rg.y), w, S0);
+                S1 = __ffma2_rn(f2(rg.z, rg.w), w, S1);
+                S2 = __ffma2_rn(f2(bt.x, bt.y), w, S2);
+                T = f2(ca ? Tb.x : T.x, cb ? Tb.y : T.y);
                 // power = p2 ln2; d power / d(dx, dy) = ln2 (2 qa dx + qb dy, 2 qc dy + qb dx)
-                const bool unclamped = contrib && raw <= kAlphaMax;
-                const float dpow = unclamped ? dA * alpha : 0.0f;
-                float gv[kG2D];
-                gv[0] = dpow * kLn2 * (2.0f * q.x * dx + q.y * dy);
-                gv[1] = dpow * kLn2 * (2.0f * q.z * dy + q.y * dx);
-                gv[2] = dpow * (-0.5f * dx * dx);
-                gv[3] = dpow * (-dx * dy);
-                gv[4] = dpow * (-0.5f * dy * dy);
-                gv[5] = unclamped ? dA * G : 0.0f;
-                gv[6] = g0 * w;
-                gv[7] = g1 * w;
-                gv[8] = g2 * w;
-                if (__any_sync(0xFFFFFFFFu, contrib)) {
-                    const float lo[8] = {gv[0], gv[1], gv[2], gv[3], gv[4], gv[5], gv[6], gv[7]};
+                const bool ua = ca && raw.x <= kAlphaMax, ub = cb && raw.y <= kAlphaMax;
+                const float2 dAa = __fmul2_rn(dA, alpha);
+                const float2 dpow = f2(ua ? dAa.x : 0.0f, ub ? dAa.y : 0.0f);
+                const float2 dpl = __fmul2_rn(dpow, ln2), hdp = __fmul2_rn(dpow, mhalf);
+                const float2 dAG = __fmul2_rn(dA, G);
+                float2 gv[kG2D];
+                gv[0] = __fmul2_rn(dpl, __fadd2_rn(t, qadx));                                  // 2 qa dx + qb dy
+                gv[1] = __fmul2_rn(dpl, __ffma2_rn(f2(qab.z, qab.w), dx, __fadd2_rn(qcdy, qcdy)));  // 2 qc dy + qb dx
+                gv[2] = __fmul2_rn(hdp, __fmul2_rn(dx, dx));
+                gv[3] = __fmul2_rn(__fmul2_rn(dpow, mone), __fmul2_rn(dx, dy));
+                gv[4] = __fmul2_rn(hdp, __fmul2_rn(dy, dy));
+                gv[5] = f2(ua ? dAG.x : 0.0f, ub ? dAG.y : 0.0f);
+                gv[6] = __fmul2_rn(g0, w);
+                gv[7] = __fmul2_rn(g1, w);
+                gv[8] = __fmul2_rn(g2, w);
+                if (__any_sync(0xFFFFFFFFu, ca || cb)) {
+                    // the lane's two pixels first, then the warp
+                    const float lo[8] = {gv[0].x + gv[0].y, gv[1].x + gv[1].y, gv[2].x + gv[2].y, gv[3].x + gv[3].y,
+                                         gv[4].x + gv[4].y, gv[5].x + gv[5].y, gv[6].x + gv[6].y, gv[7].x + gv[7].y};
                     const float rs = warp_sum8_transposed(lo, lane);
-                    float b9 = gv[8];
+                    float b9 = gv[8].x + gv[8].y;
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) b9 += __shfl_xor_sync(0xFFFFFFFFu, b9, o);
-                    if ((lane & 3u) == 0) atomicAdd(&s_acc[b][jj][lane >> 2], rs);
-                    if (lane == 0) atomicAdd(&s_acc[b][jj][8], b9);
+                    if ((lane & 3u) == 0) atomicAdd(&SM.acc[b][jj][lane >> 2], rs);
+                    if (lane == 0) atomicAdd(&SM.acc[b][jj][8], b9);
                 }
             }
         }
         __syncthreads();  // round r's sums complete; the other stage buffer is filled
         // one 16-byte vector atomic per non-zero quarter of an entry's record;
         // the thread that adds a quarter also zeroes it for round r + 2
-        for (uint32_t k = tid; k < n * 3; k += kBlendThreads) {
+        for (uint32_t k = tid; k < n * 3; k += kFwdThreads) {
             const uint32_t jj = k / 3, c = k % 3;
-            float4* slot = reinterpret_cast<float4*>(&s_acc[b][jj][0]) + c;
+            float4* slot = reinterpret_cast<float4*>(&SM.acc[b][jj][0]) + c;
             const float4 v = *slot;
             if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f) {
-                atomicAdd(reinterpret_cast<float4*>(g2d_view + size_t(s_idx[bi][jj]) * kG2DStride) + c, v);
+                atomicAdd(reinterpret_cast<float4*>(g2d_view + size_t(SM.idx[bi][jj]) * kG2DStride) + c, v);
                 *slot = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
@@ -576,7 +555,7 @@ void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s) {
                              int(sizeof(BlendBackwardSmem)));
         configured = true;
     }
-    blend_backward_kernel<<<a.n_tiles, kBlendThreads, sizeof(BlendBackwardSmem), s>>>(a);
+    blend_backward_kernel<<<a.n_tiles, kFwdThreads, sizeof(BlendBackwardSmem), s>>>(a);
 }
 
 }  // namespace tpd
