@@ -115,7 +115,8 @@ enum {
     TPD_BUF_RECORDS = 0,   /* n x 240 B */
     TPD_BUF_SPLATS = 1,    /* views x n x 48 B (splat.slang:33-39) */
     TPD_BUF_OFFSETS = 2,   /* views x n u32: exclusive scan of tile counts */
-    TPD_BUF_KEYS = 3,      /* keys u64, sorted after a frame */
+    TPD_BUF_KEYS = 3,      /* keys u64 (tile << 32 | depth bits), sorted after a frame; rebuilt from the
+                              sorted tile ids and values when asked for (waits for the stream) */
     TPD_BUF_VALUES = 4,    /* Gaussian index u32, in sorted order after a frame */
     TPD_BUF_RANGES = 5,    /* tiles x 2 u32 */
     TPD_BUF_IMAGE = 6,     /* pixels x 3 floats, views packed */

@@ -89,7 +89,9 @@ struct tpd_engine {
     float* d_ent_mats = nullptr;
     uint64_t ent_mats_cap = 0;
     uint64_t capacity = 0;
-    uint64_t* d_keys[2] = {nullptr, nullptr};
+    uint32_t* d_tiles[2] = {nullptr, nullptr};  // the frame's keys as tile ids (depth order fixed by the presort)
+    uint64_t* d_keys64 = nullptr;               // (tile | depth) keys rebuilt for read-back, on demand
+    uint64_t keys64_cap = 0;
     uint32_t* d_vals[2] = {nullptr, nullptr};
     uint64_t* d_desc_sort = nullptr;
     uint32_t* d_ranges = nullptr;
@@ -223,7 +225,7 @@ int ensure_key_capacity(tpd_engine* e, uint64_t want) {
     if (want > 0x7FFFFFFFull) return fail(e, TPD_ERR_CAPACITY, "key count exceeds 2^31-1");
     invalidate_graph(e);
     for (int b = 0; b < 2; ++b) {
-        TPD_CUDA(e, dalloc(e->d_keys[b], want));
+        TPD_CUDA(e, dalloc(e->d_tiles[b], want));
         TPD_CUDA(e, dalloc(e->d_vals[b], want));
     }
     const size_t entries = sort_desc_entries(uint32_t(want));
@@ -355,12 +357,12 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
                       e->settings.test_never_publish, s);
     mark(2);
     const uint32_t cap = uint32_t(e->capacity);
-    launch_keygen(e->d_splats, order, e->d_offsets, items, e->n, e->d_views, e->d_keys[0], e->d_vals[0], cap,
+    launch_keygen(e->d_splats, order, e->d_offsets, items, e->n, e->d_views, e->d_tiles[0], e->d_vals[0], cap,
                   e->key_bits, e->d_ranges, e->total_tiles, e->d_ctl, e->num_sms, s);
     mark(3);
     SortPlan kp;
-    kp.first_bit = 32;  // the low 32 bits (depth) are already in order
-    kp.key_bits = e->key_bits;
+    kp.first_bit = 0;  // tile ids; the depth half of the keys is already in order
+    kp.key_bits = e->key_bits - 32;
     kp.hist = e->d_ctl->sort_hist;
     kp.hist_ready = true;
     kp.ticket_base = kTicketKeySortBase;
@@ -369,7 +371,7 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     kp.threads = e->settings.sort_threads == 256 ? 256 : 512;
     kp.ranges = e->d_ranges;  // the last pass writes the tile ranges
     kp.n_tiles = e->total_tiles;
-    e->sorted_in_alt = launch_sort(e->d_keys[0], e->d_vals[0], e->d_keys[1], e->d_vals[1], cap, kp, e->d_desc_sort,
+    e->sorted_in_alt = launch_sort(e->d_tiles[0], e->d_vals[0], e->d_tiles[1], e->d_vals[1], cap, kp, e->d_desc_sort,
                                    e->d_ctl, spin, e->num_sms, s);
     mark(4);
     const int b = e->sorted_in_alt ? 1 : 0;
@@ -647,10 +649,11 @@ void tpd_destroy(tpd_engine* e) {
     dfree(e->d_desc_pre);
     dfree(e->d_ent_mats);
     for (int b = 0; b < 2; ++b) {
-        dfree(e->d_keys[b]);
+        dfree(e->d_tiles[b]);
         dfree(e->d_vals[b]);
     }
     dfree(e->d_desc_sort);
+    dfree(e->d_keys64);
     dfree(e->d_ranges);
     dfree(e->d_image);
     dfree(e->d_final_T);
@@ -1076,8 +1079,35 @@ int tpd_step_async(tpd_engine* e, const float* dL_dimage, float* g_means, float*
     return TPD_OK;
 }
 
+namespace {
+
+// The sorted (tile | depth) keys of the last frame, for read-back: the frame
+// itself sorts tile ids only (their depth order comes from the presort), and
+// a key's depth is that of its value's splat, so the keys are rebuilt here
+// into a buffer of their own, allocated on first use. Waits for the stream.
+int rebuild_keys(tpd_engine* e) {
+    cudaSetDevice(e->device);
+    if (e->keys64_cap < e->capacity) {
+        dfree(e->d_keys64);
+        e->keys64_cap = 0;
+        TPD_CUDA(e, dalloc(e->d_keys64, e->capacity));
+        e->keys64_cap = e->capacity;
+    }
+    const int b = e->sorted_in_alt ? 1 : 0;
+    launch_materialize_keys(e->d_tiles[b], e->d_vals[b], e->d_splats, e->n, e->n_views > 1 ? e->d_tile_view : nullptr,
+                            e->total_tiles, uint32_t(e->capacity), e->d_ctl, e->d_keys64, e->stream);
+    TPD_CUDA(e, cudaGetLastError());
+    return wait_stream(e);
+}
+
+}  // namespace
+
 int tpd_get_buffer(const tpd_engine* e, uint32_t which, void** ptr, uint64_t* bytes) {
     if (!e || !ptr) return TPD_ERR_ARG;
+    if (which == TPD_BUF_KEYS && e->capacity > 0) {
+        const int rc = rebuild_keys(const_cast<tpd_engine*>(e));  // a read-back cache, not engine state
+        if (rc != TPD_OK) return rc;
+    }
     const int b = e->sorted_in_alt ? 1 : 0;
     void* p = nullptr;
     uint64_t sz = 0;
@@ -1086,7 +1116,7 @@ int tpd_get_buffer(const tpd_engine* e, uint32_t which, void** ptr, uint64_t* by
         case TPD_BUF_RECORDS: p = e->d_recs; sz = uint64_t(e->n) * kRecordBytes; break;
         case TPD_BUF_SPLATS: p = e->d_splats; sz = vn * sizeof(Splat); break;
         case TPD_BUF_OFFSETS: p = e->d_offsets; sz = vn * 4; break;
-        case TPD_BUF_KEYS: p = e->d_keys[b]; sz = e->capacity * 8; break;
+        case TPD_BUF_KEYS: p = e->d_keys64; sz = e->keys64_cap * 8; break;
         case TPD_BUF_VALUES: p = e->d_vals[b]; sz = e->capacity * 4; break;
         case TPD_BUF_RANGES: p = e->d_ranges; sz = uint64_t(e->total_tiles) * 8; break;
         case TPD_BUF_IMAGE: p = e->d_image; sz = e->total_pixels * 12; break;

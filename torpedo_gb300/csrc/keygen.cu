@@ -13,6 +13,8 @@
 // owner map in shared memory, so stores are coalesced and one large Gaussian
 // does not serialise its warp. Keys and values are bit-identical to the
 // reference's.
+#include <algorithm>
+
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 #include "tpd_scan.cuh"
@@ -31,12 +33,15 @@ constexpr uint32_t kKeygenThreads = 256;
 //  2. lane l fills slots l, l + 32, ...: owner's rectangle from a per-warp
 //     table, (row, column) of the slot's index inside the rectangle, the key,
 //     one coalesced store of key and value.
-// Besides the keys it counts the digits of the tile-id passes (digit
-// positions 4.. of key_bits) into ctl->sort_hist: lanes of a store group hold
-// consecutive keys, so equal digits come in runs of neighbouring lanes and
-// each run adds its length with one shared-memory atomic. The low 32 bits of
-// a key are its depth, already ordered, so no depth digit is counted or
-// sorted. Keys past the capacity are neither written nor counted.
+// A key is stored as its tile id alone: the low 32 bits of the reference's
+// key are the depth, already in order (the items come in depth order), and
+// the depth of a key is that of its value's splat, so the sort needs only the
+// tile ids and the full keys can be rebuilt from (tile, value) when read.
+// Besides the tile ids it counts their 8-bit digits (tile_bits = key_bits -
+// 32) into ctl->sort_hist[0..]: lanes of a store group hold consecutive keys,
+// so equal digits come in runs of neighbouring lanes and each run adds its
+// length with one shared-memory atomic. Keys past the capacity are neither
+// written nor counted.
 constexpr uint32_t kKeyWindow = 256;
 constexpr uint32_t kKeygenWarps = kKeygenThreads / 32;
 
@@ -45,15 +50,14 @@ struct KeygenSmem {
     uint32_t t0[kKeygenWarps][32];             // first tile of the lane's rectangle
     uint32_t wgx[kKeygenWarps][32];            // rectangle width | view grid width << 16
     uint32_t excl[kKeygenWarps][32];           // first slot of the lane's keys (warp-relative)
-    uint32_t db[kKeygenWarps][32];             // depth bits
     uint32_t gi[kKeygenWarps][32];             // Gaussian index
-    uint32_t hist[4][256];                     // tile-id digit positions 4..7
+    uint32_t hist[4][256];                     // tile-id digits 0..3
 };
 
 __global__ void __launch_bounds__(kKeygenThreads)
     keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
                   const uint32_t* __restrict__ offsets, uint32_t n_items, uint32_t n,
-                  const ViewConst* __restrict__ views, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                  const ViewConst* __restrict__ views, uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals,
                   uint32_t capacity, uint32_t key_bits, uint32_t* __restrict__ ranges, uint32_t n_tiles,
                   FrameCtl* ctl) {
     __shared__ KeygenSmem S;
@@ -63,7 +67,8 @@ __global__ void __launch_bounds__(kKeygenThreads)
     if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
     if (ctl->status & kStatusFatal) return;
     const uint32_t count = min(ctl->depth_count, n_items);
-    const uint32_t npass = min(8u, (key_bits + 7) / 8);
+    const uint32_t tile_bits = key_bits > 32u ? key_bits - 32u : 0u;
+    const uint32_t npass = min(4u, (tile_bits + 7) / 8);  // tile-id digits
     // ranges: (0xFFFFFFFF, 0) until the key sort's last pass narrows them
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x)
         reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0xFFFFFFFFu, 0u);
@@ -76,7 +81,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
     for (uint32_t wi = warp_global; wi < nwarps; wi += warps_total) {
         const uint32_t r = wi * 32u + lane;
         // per item: first tile (row-major in its view), rect width and height, view grid width
-        uint32_t w = 1, h = 0, gx = 1, off = 0, depth_bits = 0, gi = 0, t0 = 0;
+        uint32_t w = 1, h = 0, gx = 1, off = 0, gi = 0, t0 = 0;
         if (r < count) {
             const uint32_t item = items[r];
             off = offsets[r];
@@ -89,7 +94,6 @@ __global__ void __launch_bounds__(kKeygenThreads)
                 if (texel.w > 0.0f) {
                     uint32_t x0, y0, x1, y1;
                     bounding_rect(texel.x, texel.y, texel.w, gx, grid_y(vc.height), x0, y0, x1, y1);
-                    depth_bits = __float_as_uint(texel.z);
                     if (x1 > x0 && y1 > y0) {
                         w = x1 - x0;
                         h = y1 - y0;
@@ -106,7 +110,6 @@ __global__ void __launch_bounds__(kKeygenThreads)
         S.t0[warp][lane] = t0;
         S.wgx[warp][lane] = w | (gx << 16);
         S.excl[warp][lane] = excl;
-        S.db[warp][lane] = depth_bits;
         S.gi[warp][lane] = gi;
 
         for (uint32_t c0 = 0; c0 < total; c0 += kKeyWindow) {
@@ -159,19 +162,19 @@ __global__ void __launch_bounds__(kKeygenThreads)
                     }
                     tile = S.t0[warp][j] + ty * (jwg >> 16) + uint32_t(rem);
                     const uint64_t pos = uint64_t(base) + c0 + q;
-                    keys[pos] = (uint64_t(tile) << 32) | S.db[warp][j];
+                    tiles[pos] = tile;
                     vals[pos] = S.gi[warp][j];
                 }
                 // digits: runs of equal digits among neighbouring lanes, one atomic per run
                 const uint32_t live_mask = __ballot_sync(0xFFFFFFFFu, live);
-                for (uint32_t p = 4; p < npass; ++p) {
-                    const uint32_t d = (tile >> (8u * (p - 4))) & ((1u << min(8u, key_bits - 8u * p)) - 1u);
+                for (uint32_t p = 0; p < npass; ++p) {
+                    const uint32_t d = (tile >> (8u * p)) & ((1u << min(8u, tile_bits - 8u * p)) - 1u);
                     const uint32_t dprev = __shfl_up_sync(0xFFFFFFFFu, d, 1);
                     const uint32_t starts = __ballot_sync(0xFFFFFFFFu, live && (lane == 0 || dprev != d)) & live_mask;
                     if (live && ((starts >> lane) & 1u)) {
                         const uint32_t later = starts & ~(lt | (1u << lane));  // run starts after this lane
                         const uint32_t stop = later ? uint32_t(__ffs(later) - 1) : 32u - __clz(live_mask);
-                        atomicAdd(&S.hist[p - 4][d], stop - lane);
+                        atomicAdd(&S.hist[p][d], stop - lane);
                     }
                 }
             }
@@ -180,15 +183,15 @@ __global__ void __launch_bounds__(kKeygenThreads)
         __syncwarp();  // the lane table is rewritten by the next items
     }
     __syncthreads();
-    for (uint32_t p = 4; p < npass; ++p)
+    for (uint32_t p = 0; p < npass; ++p)
         for (uint32_t d = threadIdx.x; d < 256; d += blockDim.x)
-            if (S.hist[p - 4][d]) atomicAdd(&ctl->sort_hist[p][d], S.hist[p - 4][d]);
+            if (S.hist[p][d]) atomicAdd(&ctl->sort_hist[p][d], S.hist[p][d]);
 }
 
 }  // namespace
 
 void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
-                   const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
+                   const ViewConst* views, uint32_t* tiles, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
                    uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s) {
     if (n_items == 0 || n == 0) return;
     const uint64_t warps = (uint64_t(n_items) + 31) / 32;
@@ -201,9 +204,34 @@ void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* o
     }
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
     blocks = blocks < cap ? blocks : cap;
-    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, n_items, n, views, keys, vals,
+    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, n_items, n, views, tiles, vals,
                                                               capacity, key_bits, ranges, n_tiles, ctl);
 }
 
+namespace {
+
+__global__ void materialize_keys_kernel(const uint32_t* __restrict__ tiles, const uint32_t* __restrict__ vals,
+                                        const Splat* __restrict__ splats, uint32_t n,
+                                        const uint32_t* __restrict__ tile_view, uint32_t n_tiles, uint32_t capacity,
+                                        const FrameCtl* __restrict__ ctl, uint64_t* __restrict__ keys) {
+    const uint32_t K = min(ctl->total_keys, capacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+        const uint32_t t = tiles[i], g = vals[i];
+        const uint32_t v = tile_view && t < n_tiles ? tile_view[t] : 0u;
+        const uint32_t depth = g < n ? __float_as_uint(reinterpret_cast<const float4*>(splats + size_t(v) * n + g)[1].z)
+                                     : 0xFFFFFFFFu;
+        keys[i] = (uint64_t(t) << 32) | depth;
+    }
+}
+
+}  // namespace
+
+void launch_materialize_keys(const uint32_t* tiles, const uint32_t* vals, const Splat* splats, uint32_t n,
+                             const uint32_t* tile_view, uint32_t n_tiles, uint32_t capacity, const FrameCtl* ctl,
+                             uint64_t* keys, cudaStream_t s) {
+    if (capacity == 0) return;
+    const uint32_t blocks = std::min<uint32_t>((capacity + 255) / 256, 4096u);
+    materialize_keys_kernel<<<blocks, 256, 0, s>>>(tiles, vals, splats, n, tile_view, n_tiles, capacity, ctl, keys);
+}
 
 }  // namespace tpd

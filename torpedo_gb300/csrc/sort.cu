@@ -39,7 +39,6 @@ constexpr uint32_t kSortWarps = kSortThreads / 32;
 // 8 or 4 give more, shorter partitions when the sort is too small to fill the
 // GPU with 4096-key partitions (the depth sort of 1M Gaussians).
 constexpr uint32_t kSortItemsMax = 16;
-constexpr uint32_t kSortTileMax = kSortThreads * kSortItemsMax;
 constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K (and dropped keys)
 
 // Pass kinds of onesweep_kernel. The depth sort compacts the culled items
@@ -58,10 +57,10 @@ constexpr uint32_t kHistChunk = 2048;  // keys per TMA chunk (16 KB)
 // its lanes carry consecutive digits (keys of one Gaussian's tile rectangle).
 __device__ __forceinline__ uint32_t pad16(uint32_t i) { return i + (i >> 4); }
 
-template <int kItems, int kThreads>
+template <int kItems, int kThreads, typename KeyT>
 struct OnesweepSmem {
     static constexpr uint32_t kTile = kThreads * kItems;
-    uint64_t keys[kTile + kTile / 16];
+    KeyT keys[kTile + kTile / 16];
     uint32_t vals[kTile + kTile / 16];
     uint32_t whist[kThreads / 32][kRadix];
     uint32_t gdig[kRadix];    // global exclusive digit offsets of this pass
@@ -113,8 +112,9 @@ __device__ __forceinline__ void hist_add(uint32_t* h, uint32_t d) {
     if ((threadIdx.x & 31u) == leader && d < kRadix) atomicAdd(&h[d], __popc(peers));
 }
 
+template <typename KeyT>
 __global__ void __launch_bounds__(kHistThreads)
-    sort_histogram_kernel(const uint64_t* __restrict__ keys, uint32_t capacity, uint32_t p0, uint32_t p1,
+    sort_histogram_kernel(const KeyT* __restrict__ keys, uint32_t capacity, uint32_t p0, uint32_t p1,
                           uint32_t key_bits, uint32_t (*hist)[256], FrameCtl* ctl) {
     __shared__ uint32_t sh[8][kRadix];
     const uint32_t tid = threadIdx.x;
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kHistThreads)
         for (uint32_t j = tid; j < kHistChunk; j += kHistThreads) {
             const uint32_t idx = base + j;
             const bool v = idx < K;
-            const uint64_t k = v ? keys[idx] : 0ull;
+            const uint64_t k = v ? uint64_t(keys[idx]) : 0ull;
             for (uint32_t p = p0; p < p1; ++p)
                 hist_add(sh[p], v ? (uint32_t(k >> shift[p]) & mask[p]) : kInvalidDigit);
         }
@@ -186,15 +186,16 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
 }
 
 // keys_out / vals_out [0, K) = keys_in / vals_in: thread t of nthr moves
-// 16-byte vectors (two keys, four values), kUnroll loads in flight before
-// their stores; scalar when a buffer is not 16-byte aligned.
-template <uint32_t kUnroll>
-__device__ __forceinline__ void copy_pairs(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-                                           uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t K,
+// 16-byte vectors (16 / sizeof(KeyT) keys, four values), kUnroll loads in
+// flight before their stores; scalar when a buffer is not 16-byte aligned.
+template <uint32_t kUnroll, typename KeyT>
+__device__ __forceinline__ void copy_pairs(const KeyT* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                                           KeyT* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t K,
                                            uint32_t t, uint32_t nthr) {
+    constexpr uint32_t kPerVec = 16 / sizeof(KeyT);
     const bool vec = ((reinterpret_cast<uintptr_t>(keys_in) | reinterpret_cast<uintptr_t>(keys_out) |
                        reinterpret_cast<uintptr_t>(vals_in) | reinterpret_cast<uintptr_t>(vals_out)) & 15u) == 0;
-    const uint32_t nk = vec ? K / 2 : 0u, nv = vec ? K / 4 : 0u;
+    const uint32_t nk = vec ? K / kPerVec : 0u, nv = vec ? K / 4 : 0u;
     auto copy16 = [&](const uint4* __restrict__ src, uint4* __restrict__ dst, uint32_t n) {
         for (uint32_t i0 = t; i0 < n; i0 += nthr * kUnroll) {
             uint4 r[kUnroll];
@@ -208,7 +209,7 @@ __device__ __forceinline__ void copy_pairs(const uint64_t* __restrict__ keys_in,
     };
     copy16(reinterpret_cast<const uint4*>(keys_in), reinterpret_cast<uint4*>(keys_out), nk);
     copy16(reinterpret_cast<const uint4*>(vals_in), reinterpret_cast<uint4*>(vals_out), nv);
-    for (uint32_t i = 2 * nk + t; i < K; i += nthr) keys_out[i] = keys_in[i];
+    for (uint32_t i = kPerVec * nk + t; i < K; i += nthr) keys_out[i] = keys_in[i];
     for (uint32_t i = 4 * nv + t; i < K; i += nthr) vals_out[i] = vals_in[i];
 }
 
@@ -218,21 +219,26 @@ __device__ __forceinline__ void copy_pairs(const uint64_t* __restrict__ keys_in,
 // previous key has another tile and ends where the next one has; at the
 // edges of a run the neighbour lies in another partition, and min / max
 // reductions over all candidates give the range whatever the order.
-template <int kItems, int kThreads>
-__device__ __forceinline__ void tile_range_bounds(const OnesweepSmem<kItems, kThreads>& S, uint32_t* ranges,
-                                                  uint32_t n_tiles, uint64_t key, uint32_t j, uint32_t cnt,
+// A key's tile id: the high 32 bits of a (tile | depth) key, or the whole of
+// a 32-bit tile-id key.
+__device__ __forceinline__ uint32_t tile_of(uint64_t key) { return uint32_t(key >> 32); }
+__device__ __forceinline__ uint32_t tile_of(uint32_t key) { return key; }
+
+template <int kItems, int kThreads, typename KeyT>
+__device__ __forceinline__ void tile_range_bounds(const OnesweepSmem<kItems, kThreads, KeyT>& S, uint32_t* ranges,
+                                                  uint32_t n_tiles, KeyT key, uint32_t j, uint32_t cnt,
                                                   uint32_t d, uint32_t g, uint32_t shift, uint32_t mask,
                                                   FrameCtl* ctl) {
-    const uint32_t t = uint32_t(key >> 32);
+    const uint32_t t = tile_of(key);
     if (!TPD_INBOUNDS(ctl, 18, t, n_tiles)) return;
     bool first = j == 0, last = j + 1 == cnt;
     if (!first) {
-        const uint64_t kp = S.keys[pad16(j - 1)];
-        first = (uint32_t(kp >> shift) & mask) != d || uint32_t(kp >> 32) != t;
+        const KeyT kp = S.keys[pad16(j - 1)];
+        first = (uint32_t(kp >> shift) & mask) != d || tile_of(kp) != t;
     }
     if (!last) {
-        const uint64_t kn = S.keys[pad16(j + 1)];
-        last = (uint32_t(kn >> shift) & mask) != d || uint32_t(kn >> 32) != t;
+        const KeyT kn = S.keys[pad16(j + 1)];
+        last = (uint32_t(kn >> shift) & mask) != d || tile_of(kn) != t;
     }
     if (first) atomicMin(&ranges[2 * t], g);
     if (last) atomicMax(&ranges[2 * t + 1], g + 1);
@@ -241,10 +247,12 @@ __device__ __forceinline__ void tile_range_bounds(const OnesweepSmem<kItems, kTh
 // kThreads = 256 (one digit per thread) or 512 (the digit-wide steps run on
 // the first 256 threads); a partition is kThreads * kItems keys. kPass is a
 // pass kind (kPassPlain ...): dropped keys are ranked as past-the-end keys.
-template <int kItems, int kThreads, int kMinBlocks, int kPass>
+// KeyT is uint64_t ((tile | depth) or (view | depth) keys) or uint32_t (tile
+// ids, whose depth order the depth presort has already fixed).
+template <int kItems, int kThreads, int kMinBlocks, int kPass, typename KeyT>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
-    onesweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-                    uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
+    onesweep_kernel(const KeyT* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                    KeyT* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
                     uint32_t pass, uint32_t shift, uint32_t bits, const uint32_t (*hist)[256], uint32_t ticket_slot,
                     uint32_t tag_slot, uint32_t fixed_count, uint64_t* __restrict__ desc, FrameCtl* ctl,
                     uint32_t spin_limit, uint32_t* __restrict__ ranges, uint32_t n_tiles) {
@@ -253,10 +261,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     // digits ranked with match-any in the 512-thread variant (32 warps per SM
     // hide its latency), with bit ballots otherwise (fixed cost)
     constexpr bool kMatchRank = kThreads == 512;
-    OnesweepSmem<kItems, kThreads>& S = *reinterpret_cast<OnesweepSmem<kItems, kThreads>*>(smem_raw);
+    OnesweepSmem<kItems, kThreads, KeyT>& S = *reinterpret_cast<OnesweepSmem<kItems, kThreads, KeyT>*>(smem_raw);
     const bool digit_thread = threadIdx.x < kRadix;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     constexpr bool kDrop = kPass == kPassDropCulled;
+    static_assert(kPass == kPassPlain || sizeof(KeyT) == 8, "depth-sort pass kinds take 64-bit keys");
     const uint32_t K = (ctl->status & kStatusFatal)
                            ? 0u
                            : min(kPass == kPassCompacted ? ctl->depth_count
@@ -294,14 +303,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     // registers, takes its ticket and loads at the top of each partition.
     constexpr bool kValsEarly = kItems * kMinBlocks * (kThreads / 256) <= 32;
     constexpr bool kPrefetch = kThreads == 256;
-    uint64_t k[kSortItems];
+    KeyT k[kSortItems];
     uint32_t vr[kValsEarly ? kSortItems : 1];
     auto load_partition = [&](uint32_t p) {
         const uint32_t b = p * kSortTile, c = p < nparts ? min(kSortTile, K - b) : 0u;
 #pragma unroll
         for (uint32_t i = 0; i < kSortItems; ++i) {
             const uint32_t idx = warp * (kSortItems * 32) + i * 32 + lane;
-            k[i] = idx < c ? keys_in[b + idx] : ~0ull;
+            k[i] = idx < c ? keys_in[b + idx] : KeyT(~KeyT(0));
             if constexpr (kValsEarly) vr[i] = idx < c ? vals_in[b + idx] : 0u;
         }
     };
@@ -447,7 +456,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         // coalesced write-out of digit runs
         const uint32_t cntv = kDrop ? S.valid : cnt;
         for (uint32_t j = tid; j < cntv; j += kThreads) {
-            const uint64_t key = S.keys[pad16(j)];
+            const KeyT key = S.keys[pad16(j)];
             const uint32_t d = uint32_t(key >> shift) & mask;
             const uint32_t g = S.gmap[d] + j;
             if (g < capacity && TPD_INBOUNDS(ctl, 17, g, K + (K == 0))) {
@@ -464,40 +473,45 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 // (128 registers, no spills; the default) or 3 (80 registers); the 512-thread,
 // 8-key variant for 2 (32 warps per SM); the 8- and 4-key 256-thread variants
 // (shorter partitions, for small sorts) for 4 and 5.
-template <int kItems, int kThreads, int kMinBlocks>
+template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
 int onesweep_occupancy() {
     static int b = 0;
     if (b == 0) {
-        const size_t smem = sizeof(OnesweepSmem<kItems, kThreads>);
-        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain>,
+        const size_t smem = sizeof(OnesweepSmem<kItems, kThreads, KeyT>);
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain, KeyT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if constexpr (sizeof(KeyT) == 8) {
+            cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled, KeyT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted, KeyT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        }
         int r = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain, KeyT>,
                                                       kThreads, smem);
         b = r > 0 ? r : 1;
     }
     return b;
 }
 
-template <int kItems, int kThreads, int kMinBlocks>
-void launch_passes(uint64_t* kin, uint32_t* vin, uint64_t* kout, uint32_t* vout, uint32_t capacity, uint32_t p0,
+template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+void launch_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_t capacity, uint32_t p0,
                    uint32_t p1, const SortPlan& plan, uint32_t (*hist)[256], uint64_t* desc, FrameCtl* ctl,
                    uint32_t spin_limit, int sms, cudaStream_t s) {
-    const size_t smem = sizeof(OnesweepSmem<kItems, kThreads>);
-    const int occ = onesweep_occupancy<kItems, kThreads, kMinBlocks>();
+    const size_t smem = sizeof(OnesweepSmem<kItems, kThreads, KeyT>);
+    const int occ = onesweep_occupancy<kItems, kThreads, kMinBlocks, KeyT>();
     const uint32_t tile = kThreads * kItems;
     const uint32_t max_parts = (capacity + tile - 1) / tile;
     const uint32_t grid = std::max(1u, std::min<uint32_t>(max_parts, uint32_t(sms * occ)));
     for (uint32_t p = p0; p < p1; ++p) {
         const uint32_t shift = p * kRadixBits;
         const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
-        auto kernel = !plan.compact_culled ? onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain>
-                      : p == p0            ? onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled>
-                                           : onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted>;
+        auto kernel = onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain, KeyT>;
+        if constexpr (sizeof(KeyT) == 8) {
+            if (plan.compact_culled)
+                kernel = p == p0 ? onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled, KeyT>
+                                 : onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted, KeyT>;
+        }
         kernel<<<grid, kThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p,
                                             plan.tag_base + p, plan.fixed_count, desc, ctl, spin_limit,
                                             p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles);
@@ -517,7 +531,9 @@ size_t sort_desc_entries(uint32_t capacity, uint32_t items) {
 
 void launch_sort_begin(FrameCtl* ctl, uint32_t total, cudaStream_t s) { sort_begin_kernel<<<1, 256, 0, s>>>(ctl, total); }
 
-bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
+namespace {
+template <typename KeyT>
+bool launch_sort_t(KeyT* keys, uint32_t* vals, KeyT* keys_alt, uint32_t* vals_alt, uint32_t capacity,
                  const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
                  cudaStream_t s) {
     const uint32_t p0 = plan.first_bit / kRadixBits;
@@ -546,6 +562,19 @@ bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* v
         launch_passes<16, 256, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
                                   sms, s);
     return ((p1 - p0) & 1u) != 0;
+}
+}  // namespace
+
+bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
+                 const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 cudaStream_t s) {
+    return launch_sort_t(keys, vals, keys_alt, vals_alt, capacity, plan, desc, ctl, spin_limit, num_sms, s);
+}
+
+bool launch_sort(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
+                 const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 cudaStream_t s) {
+    return launch_sort_t(keys, vals, keys_alt, vals_alt, capacity, plan, desc, ctl, spin_limit, num_sms, s);
 }
 
 }  // namespace tpd

@@ -75,15 +75,25 @@ void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t max_
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
                        uint32_t spin_limit, uint32_t never_publish, cudaStream_t s);
 
-// keygen.slang: keys = (tile_base + tile) << 32 | bits(viewZ), vals = Gaussian
-// index, for the items[] in depth order with their key offsets. K is read from
-// ctl->total_keys; keys beyond capacity are dropped and flagged. Also counts the
-// digits of the tile-id passes (digit positions 4.. of key_bits) into ctl->sort_hist.
-// Also presets ranges (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
+// keygen.slang's keys (tile_base + tile) << 32 | bits(viewZ) and vals = Gaussian
+// index, for the items[] in depth order with their key offsets. The items come
+// in depth order, so only the tile id of each key is written (tiles[], u32):
+// the depth half of a key is the depth of its value's splat
+// (launch_materialize_keys). K is read from ctl->total_keys; keys beyond
+// capacity are dropped and flagged. Also counts the 8-bit digits of the tile
+// ids (tile_bits = key_bits - 32) into ctl->sort_hist[0..], and presets ranges
+// (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
 // items[0 .. ctl->depth_count) index the n_items = n_views x n splats.
 void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
-                   const ViewConst* views, uint64_t* keys, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
+                   const ViewConst* views, uint32_t* tiles, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
                    uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s);
+
+// keys[i] = tiles[i] << 32 | bits(viewZ of splat vals[i] in the tile's view),
+// i < min(ctl->total_keys, capacity): the 64-bit (tile | depth) keys of a
+// frame, from its sorted tile ids and values (read-back only).
+void launch_materialize_keys(const uint32_t* tiles, const uint32_t* vals, const Splat* splats, uint32_t n,
+                             const uint32_t* tile_view, uint32_t n_tiles, uint32_t capacity, const FrameCtl* ctl,
+                             uint64_t* keys, cudaStream_t s);
 
 // Onesweep LSD radix sort of (key, val) pairs on key bits [first_bit, key_bits),
 // first_bit a multiple of 8. K = min(ctl->total_keys, capacity). hist: the
@@ -114,6 +124,10 @@ struct SortPlan {
     cudaEvent_t after_hist = nullptr;  // recorded between the histogram and the first pass
 };
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
+                 const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
+                 cudaStream_t s);
+// The same for 32-bit keys (the frame's tile ids).
+bool launch_sort(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
                  const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
                  cudaStream_t s);
 // Clears status, histograms and tickets, sets total_keys and advances the tag
