@@ -379,8 +379,9 @@ __global__ void __launch_bounds__(kFwdThreads, kBwdMinBlocks) blend_backward_ker
     extern __shared__ __align__(16) unsigned char bwd_smem[];
     BlendBackwardSmem& SM = *reinterpret_cast<BlendBackwardSmem*>(bwd_smem);
 
-    const uint32_t tile = blockIdx.x;
+    const uint32_t tile = a.tile_order ? a.tile_order[blockIdx.x] : blockIdx.x;
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
+    if (!TPD_INBOUNDS(a.ctl, 44, tile, a.n_tiles)) return;
     uint32_t vi, W, H, tx, ty;
     load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -535,7 +536,48 @@ __global__ void __launch_bounds__(kFwdThreads, kBwdMinBlocks) blend_backward_ker
     }
 }
 
+// One CTA: a counting sort of the tiles into 32 classes of list length
+// (floor(log2(length + 1)), longest class first).
+constexpr uint32_t kOrderThreads = 1024;
+
+__global__ void __launch_bounds__(kOrderThreads)
+    tile_order_kernel(const uint32_t* __restrict__ ranges, uint32_t n_tiles, const FrameCtl* __restrict__ ctl,
+                      uint32_t capacity, uint32_t* __restrict__ order) {
+    __shared__ uint32_t count[32], base[32];
+    const uint32_t tid = threadIdx.x;
+    if (tid < 32) count[tid] = 0;
+    __syncthreads();
+    const uint32_t K = min(ctl->total_keys, capacity);
+    // class c = floor(log2(len + 1)) in 0..31; slot 31 - c puts long lists first
+    auto slot = [&](uint32_t t) {
+        const uint32_t end = min(ranges[2 * t + 1], K), start = min(ranges[2 * t], end);
+        const uint32_t len = end - start;
+        const uint32_t c = 31u - __clz(len + 1u);  // len < 2^31
+        return 31u - c;
+    };
+    for (uint32_t t = tid; t < n_tiles; t += kOrderThreads) atomicAdd(&count[slot(t)], 1u);
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t run = 0;
+        for (uint32_t c = 0; c < 32; ++c) {
+            base[c] = run;
+            run += count[c];
+        }
+    }
+    __syncthreads();
+    for (uint32_t t = tid; t < n_tiles; t += kOrderThreads) {
+        const uint32_t pos = atomicAdd(&base[slot(t)], 1u);
+        if (pos < n_tiles) order[pos] = t;
+    }
+}
+
 }  // namespace
+
+void launch_tile_order(const uint32_t* ranges, uint32_t n_tiles, const FrameCtl* ctl, uint32_t capacity,
+                       uint32_t* order, cudaStream_t s) {
+    if (n_tiles == 0) return;
+    tile_order_kernel<<<1, kOrderThreads, 0, s>>>(ranges, n_tiles, ctl, capacity, order);
+}
 
 void launch_blend(const BlendArgs& a, cudaStream_t s) {
     if (a.n_tiles == 0) return;

@@ -73,6 +73,7 @@ struct tpd_engine {
     uint32_t total_tiles = 0;
     uint64_t total_pixels = 0;
     uint32_t* d_tile_view = nullptr;
+    uint32_t* d_tile_order = nullptr;  // tiles by decreasing list length, for the blend adjoint
     uint64_t* d_image_offset = nullptr;
 
     // frame buffers
@@ -475,6 +476,7 @@ int set_views_internal(tpd_engine* e, const tpd_view* views, uint32_t nv) {
     if (tiles > e->tile_cap) {
         TPD_CUDA(e, dalloc(e->d_ranges, uint64_t(tiles) * 2));
         TPD_CUDA(e, dalloc(e->d_tile_view, tiles));
+        TPD_CUDA(e, dalloc(e->d_tile_order, tiles));
         e->tile_cap = tiles;
     }
     if (!e->d_image_offset) TPD_CUDA(e, dalloc(e->d_image_offset, kMaxViews));
@@ -638,6 +640,7 @@ void tpd_destroy(tpd_engine* e) {
     dfree(e->d_transforms);
     dfree(e->d_views);
     dfree(e->d_tile_view);
+    dfree(e->d_tile_order);
     dfree(e->d_image_offset);
     dfree(e->d_splats);
     dfree(e->d_offsets);
@@ -1003,6 +1006,9 @@ void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& 
     bb.dL_dimage = dL_dimage;
     bb.g2d = e->d_g2d;
     bb.g2d_view_stride = uint64_t(e->n) * kG2DStride;
+    // longest tile lists first: the adjoint's cost per tile varies more than the forward's
+    launch_tile_order(e->d_ranges, e->total_tiles, e->d_ctl, uint32_t(e->capacity), e->d_tile_order, e->stream);
+    bb.tile_order = e->d_tile_order;
     launch_blend_backward(bb, e->stream);
     PreprocessBackwardArgs pb{};
     pb.recs = e->d_recs;

@@ -172,8 +172,17 @@ struct BlendBackwardArgs {
     const float* dL_dimage;   // HWC float3
     float* g2d;               // n x kG2DStride (px, py, conic.xyz, opacity, rgb, 3 pad), accumulated
     uint64_t g2d_view_stride; // floats between views' g2d (n * kG2DStride)
+    const uint32_t* tile_order;  // nullable: CTA b differentiates tile tile_order[b] (launch_tile_order)
 };
 void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s);
+
+// order[0 .. n_tiles): the tiles by decreasing list length (in classes of
+// equal floor(log2(length + 1)); any order within a class), so the longest
+// lists start first and no SM is left with one at the end. ranges as the
+// blend leaves them (empty tiles (0, 0)); lengths are clipped at
+// min(ctl->total_keys, capacity).
+void launch_tile_order(const uint32_t* ranges, uint32_t n_tiles, const FrameCtl* ctl, uint32_t capacity,
+                       uint32_t* order, cudaStream_t s);
 
 // Per-splat gradient record of the blend adjoint: 9 used floats padded to 12
 // (48 B), so it is accumulated with three 16-byte vector atomics.
