@@ -499,10 +499,17 @@ def run_ours(args):
         "warmup": max(3, args.warmup), "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded cfg1 generator)",
         "config": workload_config(cfg, cam, K),
-        "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit radix pass)",
+        "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit tile-id radix pass of the key sort)",
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_kind": f"{peak_kind} copy bandwidth",
-                     "bytes_per_launch": K * 24, "avg_launch_ms": round(pass_ms, 5)},
+                     "bytes_per_launch": K * 24, "avg_launch_ms": round(pass_ms, 5),
+                     "basis": "K * 24 B per 8-bit pass: the per-pass term of the fixed sort formula "
+                              "K * (8 + 24 * ceil(B / 8)) for 64-bit keys and 32-bit values",
+                     "moved_bytes_per_launch": K * 16,
+                     "moved_GBps": round(K * 16 / (pass_ms / 1000.0) / 1e9, 1),
+                     "moved_frac": round(K * 16 / (pass_ms / 1000.0) / 1e9 / hbm, 4),
+                     "moved_note": "the pass itself reads and writes 32-bit tile ids and 32-bit values "
+                                   "(16 B per key); the depth half of the keys is ordered by the depth presort"},
         "frame_sort": {"keys": K, "key_bits": key_bits, "tile_passes": passes,
                        "depth_sort_ms": round(stage_avg["depth_sort"], 4), "key_sort_ms": round(stage_avg["key_sort"], 4),
                        "formula_GBps": round(sort_formula / ((stage_avg["depth_sort"] + stage_avg["key_sort"]) / 1000) / 1e9, 1),
