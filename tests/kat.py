@@ -112,3 +112,22 @@ def tiny_view():
     recs = np.stack([record((float(x), float(y), float(z)), 0.7, (0.04, 0.05, 0.03), sh=rgb2sh(0.9, 0.5, 0.1))
                      for x, y, z in np.random.default_rng(12).normal(0, 0.2, (300, 3))])
     return recs, camera(5, 3)
+
+
+def thin_rotated():
+    """400 needle-like Gaussians (one long axis of 0.3-2 world units, the other
+    two 0.002-0.01), randomly rotated, half of them with opacity just above
+    1/255, over a 256x256 view: alpha >= 1/255 regions that are long, thin
+    and diagonal, where a conservative per-block cull is easiest to get wrong."""
+    rng = np.random.default_rng(13)
+    recs = []
+    for _ in range(400):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        scale = rng.uniform(0.002, 0.01, 3)
+        scale[int(rng.integers(0, 3))] = rng.uniform(0.3, 2.0)
+        op = float(rng.uniform(1.0 / 255, 1.3 / 255)) if rng.random() < 0.5 else float(rng.uniform(0.3, 0.99))
+        pos = (float(rng.uniform(-2.5, 2.5)), float(rng.uniform(-2.5, 2.5)), float(rng.uniform(-1.0, 1.0)))
+        recs.append(record(pos, op, tuple(float(s) for s in scale), quat=tuple(float(v) for v in q),
+                           sh=rgb2sh(*(float(c) for c in rng.uniform(0, 1, 3)))))
+    return np.stack(recs), camera()
