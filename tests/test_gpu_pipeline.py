@@ -44,13 +44,11 @@ def _scene(name):
         return kat.screen_filling()
     if name == "kat_tiny_view":
         return kat.tiny_view()
-    if name == "kat_thin_rotated":
-        return kat.thin_rotated()
     raise KeyError(name)
 
 
 SCENES = ["cfg0", "cfg1_200k", "cfg2_50k", "odd_size", "kat_single", "kat_two", "kat_edge", "kat_culled",
-          "kat_screen_filling", "kat_tiny_view", "kat_thin_rotated"]
+          "kat_screen_filling", "kat_tiny_view"]
 _cache = {}
 
 
@@ -124,6 +122,42 @@ def test_final_T_and_contributors(frame):
     ok = ~o["pfrag"]
     assert np.abs(T_[ok] - o["T64"][ok]).max(initial=0.0) <= 1e-3
     assert np.mean(nc[ok] == o["nc64"][ok]) >= 0.999
+
+
+def test_thin_rotated_needles(cuda):
+    """Long, thin, rotated Gaussians (kat.thin_rotated): the case where the
+    blend's per-block cull is easiest to get wrong. Their FP32 conics carry
+    up to 2e-3 relative error against FP64 (condition numbers near 3e4), the
+    reference's own FP32 arithmetic, so the blend is checked against an FP64
+    blend of the exact FP32 splats instead: a contributing pair that the cull
+    dropped would change the contributor count, T and colour of the pixels
+    along a needle's edge, far more than the few pixels where an FP32 decision
+    near a threshold goes the other way."""
+    from oracle import oracle as O
+
+    recs, cam = kat.thin_rotated()
+    eng, stats = H.render(recs, [cam])
+    g = H.gpu_state(eng, stats)
+    eng.close()
+    o = H.oracle_frame(recs, cam, f64=False)
+    np.testing.assert_array_equal(g["splats"], o["s32"])
+    np.testing.assert_array_equal(g["keys"], o["keys"])
+    np.testing.assert_array_equal(g["vals"], o["vals"])
+    np.testing.assert_array_equal(g["ranges"], o["ranges"])
+    s = o["s32"]
+    s64 = s.view(np.float32).astype(np.float64)
+    s64[:, 3] = s[:, 3].astype(np.float64)
+    img64, T64, nc64, pfrag = O.blend_f64(s64, o["vals"], o["ranges"], cam.width, cam.height)
+    ok = ~pfrag
+    err = np.abs(g["images"][0].astype(np.float64) - img64).max(axis=2)[ok]
+    T_ = g["final_T"].reshape(cam.height, cam.width).astype(np.float64)[ok]
+    nc = g["n_contrib"].reshape(cam.height, cam.width)[ok]
+    n = err.size
+    print(f"thin needles: K={stats['keys']}, pixels > 1e-3: {int((err > 1e-3).sum())} of {n}, "
+          f"max {err.max():.2e}; contributor counts equal: {np.mean(nc == nc64[ok]):.5f}")
+    assert (err > tol.IMAGE_ABS).sum() <= n // 1000
+    assert (np.abs(T_ - T64[ok]) > 1e-3).sum() <= n // 1000
+    assert np.mean(nc == nc64[ok]) >= 0.999
 
 
 @pytest.mark.parametrize("deg", [0, 1, 2, 3])

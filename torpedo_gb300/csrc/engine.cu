@@ -334,6 +334,7 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     pa.depth_keys = e->d_dkeys[0];
     pa.depth_items = e->d_ditems[0];
     pa.depth_key_bits = e->depth_key_bits;
+    pa.tile_bits = e->key_bits - 32;  // the key sort's digit counts
     pa.ctl = e->d_ctl;
     launch_preprocess(pa, e->num_sms, s);
     mark(1);
@@ -363,6 +364,7 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     mark(3);
     SortPlan kp;
     kp.first_bit = 0;  // tile ids; the depth half of the keys is already in order
+    kp.skip_on_overflow = true;
     kp.key_bits = e->key_bits - 32;
     kp.hist = e->d_ctl->sort_hist;
     kp.hist_ready = true;

@@ -37,11 +37,9 @@ constexpr uint32_t kKeygenThreads = 256;
 // key are the depth, already in order (the items come in depth order), and
 // the depth of a key is that of its value's splat, so the sort needs only the
 // tile ids and the full keys can be rebuilt from (tile, value) when read.
-// Besides the tile ids it counts their 8-bit digits (tile_bits = key_bits -
-// 32) into ctl->sort_hist[0..]: lanes of a store group hold consecutive keys,
-// so equal digits come in runs of neighbouring lanes and each run adds its
-// length with one shared-memory atomic. Keys past the capacity are neither
-// written nor counted.
+// Keys past the capacity are not written (the frame is flagged and rendered
+// again). The digit counts of the tile ids come from the preprocess, which
+// counts each Gaussian's tile rectangle row by row.
 constexpr uint32_t kKeyWindow = 256;
 constexpr uint32_t kKeygenWarps = kKeygenThreads / 32;
 
@@ -51,7 +49,6 @@ struct KeygenSmem {
     uint32_t wgx[kKeygenWarps][32];            // rectangle width | view grid width << 16
     uint32_t excl[kKeygenWarps][32];           // first slot of the lane's keys (warp-relative)
     uint32_t gi[kKeygenWarps][32];             // Gaussian index
-    uint32_t hist[4][256];                     // tile-id digits 0..3
 };
 
 __global__ void __launch_bounds__(kKeygenThreads)
@@ -67,16 +64,11 @@ __global__ void __launch_bounds__(kKeygenThreads)
     if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
     if (ctl->status & kStatusFatal) return;
     const uint32_t count = min(ctl->depth_count, n_items);
-    const uint32_t tile_bits = key_bits > 32u ? key_bits - 32u : 0u;
-    const uint32_t npass = min(4u, (tile_bits + 7) / 8);  // tile-id digits
     // ranges: (0xFFFFFFFF, 0) until the key sort's last pass narrows them
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x)
         reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0xFFFFFFFFu, 0u);
-    for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x) (&S.hist[0][0])[k] = 0;
-    __syncthreads();
     uint32_t* owner = S.owner[warp];
     const uint32_t nwarps = (count + 31) / 32;
-    const uint32_t lt = (1u << lane) - 1u;
 
     for (uint32_t wi = warp_global; wi < nwarps; wi += warps_total) {
         const uint32_t r = wi * 32u + lane;
@@ -142,10 +134,8 @@ __global__ void __launch_bounds__(kKeygenThreads)
             for (uint32_t q = 0; q < kKeyWindow / 32; ++q) owner[lane * (kKeyWindow / 32) + q] = max(before, mine[q]);
             __syncwarp();
             // 2. slots lane, lane + 32, ...: one coalesced store group per step
-            for (uint32_t q = lane; q - lane < span; q += 32u) {
-                const bool live = q < span && uint64_t(base) + c0 + q < capacity;
-                uint32_t tile = 0;
-                if (live) {
+            for (uint32_t q = lane; q < span; q += 32u) {
+                if (uint64_t(base) + c0 + q < capacity) {
                     const uint32_t j = owner[q];
                     const uint32_t local = c0 + q - S.excl[warp][j];  // < 2^24: exact in a float
                     const uint32_t jwg = S.wgx[warp][j];
@@ -160,32 +150,16 @@ __global__ void __launch_bounds__(kKeygenThreads)
                         ++ty;
                         rem -= int32_t(jw);
                     }
-                    tile = S.t0[warp][j] + ty * (jwg >> 16) + uint32_t(rem);
+                    const uint32_t tile = S.t0[warp][j] + ty * (jwg >> 16) + uint32_t(rem);
                     const uint64_t pos = uint64_t(base) + c0 + q;
                     tiles[pos] = tile;
                     vals[pos] = S.gi[warp][j];
-                }
-                // digits: runs of equal digits among neighbouring lanes, one atomic per run
-                const uint32_t live_mask = __ballot_sync(0xFFFFFFFFu, live);
-                for (uint32_t p = 0; p < npass; ++p) {
-                    const uint32_t d = (tile >> (8u * p)) & ((1u << min(8u, tile_bits - 8u * p)) - 1u);
-                    const uint32_t dprev = __shfl_up_sync(0xFFFFFFFFu, d, 1);
-                    const uint32_t starts = __ballot_sync(0xFFFFFFFFu, live && (lane == 0 || dprev != d)) & live_mask;
-                    if (live && ((starts >> lane) & 1u)) {
-                        const uint32_t later = starts & ~(lt | (1u << lane));  // run starts after this lane
-                        const uint32_t stop = later ? uint32_t(__ffs(later) - 1) : 32u - __clz(live_mask);
-                        atomicAdd(&S.hist[p][d], stop - lane);
-                    }
                 }
             }
             __syncwarp();  // the owner map is rebuilt for the next window
         }
         __syncwarp();  // the lane table is rewritten by the next items
     }
-    __syncthreads();
-    for (uint32_t p = 0; p < npass; ++p)
-        for (uint32_t d = threadIdx.x; d < 256; d += blockDim.x)
-            if (S.hist[p][d]) atomicAdd(&ctl->sort_hist[p][d], S.hist[p][d]);
 }
 
 }  // namespace

@@ -242,12 +242,47 @@ __device__ __forceinline__ uint32_t project_one(const Rec& rec, const float* em,
 constexpr uint32_t kPreStages = 2;
 constexpr uint32_t kDepthPassesMax = 5;  // depth keys: 32 bits + log2(256 views)
 
+constexpr uint32_t kTileDigitsMax = 4;   // tile ids: at most 32 bits
+
 struct PreSmem {
     float rec[kPreStages][kPreThreads * kRecordFloats];  // 30,720 B per stage, 16-byte multiple
     uint32_t hist[kDepthPassesMax][256];                  // depth-key digit counts of this CTA
+    // tile-id digit counts of this CTA: digit 0 as a difference array over
+    // the 256 values (+ tall added to every value), the others directly
+    uint32_t tdiff[257];
+    uint32_t tall;
+    uint32_t thist[kTileDigitsMax - 1][256];
     uint64_t bar[kPreStages];
     uint32_t kept;                                        // depth keys of visible items in this CTA
 };
+
+// Adds the w consecutive tile ids a0 .. a0 + w - 1 (one row of a Gaussian's
+// tile rectangle, all below 2^tile_bits) to the CTA's digit counts of the
+// key sort: digit 0 (t & 255) takes w / 256 on every value and a range of
+// w % 256 values (wrapping) in the difference array; digit p >= 1 takes, for
+// each value v of t >> 8p in the row, the number of ids with that value.
+__device__ __forceinline__ void count_tile_row(PreSmem& S, uint32_t a0, uint32_t w, uint32_t ndig) {
+    if (w >= 256u) atomicAdd(&S.tall, w >> 8);
+    const uint32_t rem = w & 255u;
+    if (rem) {
+        const uint32_t st = a0 & 255u, e = st + rem;
+        atomicAdd(&S.tdiff[st], 1u);
+        if (e <= 256u) {
+            atomicAdd(&S.tdiff[e], 0xFFFFFFFFu);  // -1 (tdiff[256] is never read)
+        } else {
+            atomicAdd(&S.tdiff[0], 1u);
+            atomicAdd(&S.tdiff[e - 256u], 0xFFFFFFFFu);
+        }
+    }
+    const uint64_t end = uint64_t(a0) + w;
+    for (uint32_t p = 1; p < ndig; ++p) {
+        const uint32_t sh = 8u * p;
+        for (uint64_t v = a0 >> sh; (v << sh) < end; ++v) {
+            const uint64_t lo = max(uint64_t(a0), v << sh), hi = min(end, (v + 1) << sh);
+            atomicAdd(&S.thist[p - 1][uint32_t(v) & 255u], uint32_t(hi - lo));
+        }
+    }
+}
 
 __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs a) {
     extern __shared__ __align__(128) unsigned char pre_smem[];
@@ -255,6 +290,10 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
 
     const uint32_t tid = threadIdx.x;
     for (uint32_t k = tid; k < kDepthPassesMax * 256; k += kPreThreads) (&S.hist[0][0])[k] = 0;
+    for (uint32_t k = tid; k < 257; k += kPreThreads) S.tdiff[k] = 0;
+    for (uint32_t k = tid; k < (kTileDigitsMax - 1) * 256; k += kPreThreads) (&S.thist[0][0])[k] = 0;
+    if (tid == 0) S.tall = 0;
+    const uint32_t ndig = min(kTileDigitsMax, (a.tile_bits + 7) / 8);  // 0: no tile-digit counts
     if (tid == 0) S.kept = 0;
     uint32_t kept = 0;  // this thread's visible items (the depth sort drops the others)
     if (tid == 0) {
@@ -317,9 +356,38 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
                         }
                     }
                 }
+                if (tiles && ndig) {
+                    // the keys this item will emit: its tile rectangle as key
+                    // duplication computes it from the stored splat
+                    const ViewConst& vc = a.views[v];
+                    const uint32_t gx = grid_x(vc.width);
+                    uint32_t x0, y0, x1, y1;
+                    bounding_rect(sp.px, sp.py, sp.radius, gx, grid_y(vc.height), x0, y0, x1, y1);
+                    if (sp.radius > 0.0f && x1 > x0 && y1 > y0)
+                        for (uint32_t y = y0; y < y1; ++y) count_tile_row(S, vc.tile_base + y * gx + x0, x1 - x0, ndig);
+                }
             }
         }
         __syncthreads();  // every thread is done with this stage before it is refilled
+    }
+    if (ndig) {
+        __syncthreads();
+        // digit 0: inclusive prefix of the difference array (two values per
+        // thread, 128 threads), plus the counts added to every value
+        const uint32_t d0 = 2u * tid, d1 = d0 + 1u;
+        const uint32_t v0 = S.tdiff[d0], pair = v0 + S.tdiff[d1];
+        const uint32_t incl = warp_inclusive_scan(pair);
+        __shared__ uint32_t wsum[kPreThreads / 32];
+        if ((tid & 31u) == 31u) wsum[tid >> 5] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t w = 0; w < (tid >> 5); ++w) before += wsum[w];
+        const uint32_t c1 = before + incl + S.tall, c0 = c1 - S.tdiff[d1];
+        if (c0) atomicAdd(&a.ctl->sort_hist[0][d0], c0);
+        if (c1) atomicAdd(&a.ctl->sort_hist[0][d1], c1);
+        for (uint32_t p = 1; p < ndig; ++p)
+            for (uint32_t d = tid; d < 256; d += kPreThreads)
+                if (S.thist[p - 1][d]) atomicAdd(&a.ctl->sort_hist[p][d], S.thist[p - 1][d]);
     }
     if (!a.depth_keys) return;
     kept = warp_sum(kept);

@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     KeyT* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t capacity,
                     uint32_t pass, uint32_t shift, uint32_t bits, const uint32_t (*hist)[256], uint32_t ticket_slot,
                     uint32_t tag_slot, uint32_t fixed_count, uint64_t* __restrict__ desc, FrameCtl* ctl,
-                    uint32_t spin_limit, uint32_t* __restrict__ ranges, uint32_t n_tiles) {
+                    uint32_t spin_limit, uint32_t* __restrict__ ranges, uint32_t n_tiles, uint32_t abort_mask) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr uint32_t kSortItems = kItems, kSortTile = kThreads * kItems, kWarps = kThreads / 32;
     // digits ranked with match-any in the 512-thread variant (32 warps per SM
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     constexpr bool kDrop = kPass == kPassDropCulled;
     static_assert(kPass == kPassPlain || sizeof(KeyT) == 8, "depth-sort pass kinds take 64-bit keys");
-    const uint32_t K = (ctl->status & kStatusFatal)
+    const uint32_t K = (ctl->status & abort_mask)
                            ? 0u
                            : min(kPass == kPassCompacted ? ctl->depth_count
                                                          : (fixed_count ? fixed_count : ctl->total_keys),
@@ -517,7 +517,8 @@ void launch_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_
         }
         kernel<<<grid, kThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p,
                                             plan.tag_base + p, plan.fixed_count, desc, ctl, spin_limit,
-                                            p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles);
+                                            p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles,
+                                            kStatusFatal | (plan.skip_on_overflow ? kStatusKeyOverflow : 0u));
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

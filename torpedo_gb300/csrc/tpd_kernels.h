@@ -53,6 +53,9 @@ struct PreprocessArgs {
     uint64_t* depth_keys;
     uint32_t* depth_items;
     uint32_t depth_key_bits;  // 32 + bits of (n_views - 1); its digit histograms go to ctl->depth_hist
+    // > 0: the 8-bit digit counts of the frame's tile ids (all keys the
+    // visible items will emit, tile ids below 2^tile_bits) go to ctl->sort_hist[0..]
+    uint32_t tile_bits;
     FrameCtl* ctl;
 };
 
@@ -80,9 +83,9 @@ void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint6
 // in depth order, so only the tile id of each key is written (tiles[], u32):
 // the depth half of a key is the depth of its value's splat
 // (launch_materialize_keys). K is read from ctl->total_keys; keys beyond
-// capacity are dropped and flagged. Also counts the 8-bit digits of the tile
-// ids (tile_bits = key_bits - 32) into ctl->sort_hist[0..], and presets ranges
-// (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
+// capacity are dropped and flag the frame (kStatusKeyOverflow). Also presets
+// ranges (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
+// The digit counts of the tile ids come from the preprocess (tile_bits).
 // items[0 .. ctl->depth_count) index the n_items = n_views x n splats.
 void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
                    const ViewConst* views, uint32_t* tiles, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
@@ -117,6 +120,9 @@ struct SortPlan {
     uint32_t* ranges = nullptr;        // key sort: the last pass also writes the tile ranges (preset by keygen)
     uint32_t n_tiles = 0;
     uint32_t fixed_count = 0;          // nonzero: sort this many pairs, else min(ctl->total_keys, capacity)
+    // a frame whose keys overflowed the capacity (its histograms count keys
+    // that were not written) sorts nothing; it is rendered again
+    bool skip_on_overflow = false;
     // depth sort: the first pass drops the keys whose low 32 bits are
     // 0xFFFFFFFF (culled items) and keeps ctl->depth_count, which the later
     // passes sort; a later pass whose digit is the same for every key copies
