@@ -104,9 +104,11 @@ struct Rec {
     __device__ __forceinline__ float4 f4(int q) const { return reinterpret_cast<const float4*>(p)[q]; }
 };
 
-// project() for one Gaussian. Returns the tile count (0 when culled) and fills s.
+// project() for one Gaussian. Returns the tile count (0 when culled) and fills
+// s; rect gets the tile rectangle (x0, y0, x1, y1) when the count is not 0,
+// the one key duplication derives from the stored splat's px, py and radius.
 __device__ __forceinline__ uint32_t project_one(const Rec& rec, const float* em, const ViewConst& v,
-                                                uint32_t deg, bool compat, Splat& s) {
+                                                uint32_t deg, bool compat, Splat& s, uint4& rect) {
     s = Splat{0.f, 0.f, 0.f, 0u, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const float4 pos_op = rec.f4(0);
     const float mean[3] = {pos_op.x, pos_op.y, pos_op.z};
@@ -177,6 +179,7 @@ __device__ __forceinline__ uint32_t project_one(const Rec& rec, const float* em,
     bounding_rect(px, py, radius, grid_x(v.width), grid_y(v.height), x0, y0, x1, y1);
     const uint32_t touched = (x1 - x0) * (y1 - y0);
     if (touched == 0) return 0;
+    rect = make_uint4(x0, y0, x1, y1);
 
     // camera position (common.slang:88-92) and view direction from the pre-model mean
     float campos[3];
@@ -274,12 +277,15 @@ __device__ __forceinline__ void count_tile_row(PreSmem& S, uint32_t a0, uint32_t
             atomicAdd(&S.tdiff[e - 256u], 0xFFFFFFFFu);
         }
     }
-    const uint64_t end = uint64_t(a0) + w;
+    const uint32_t last = a0 + (w - 1u);  // tile ids stay below 2^31
     for (uint32_t p = 1; p < ndig; ++p) {
-        const uint32_t sh = 8u * p;
-        for (uint64_t v = a0 >> sh; (v << sh) < end; ++v) {
-            const uint64_t lo = max(uint64_t(a0), v << sh), hi = min(end, (v + 1) << sh);
-            atomicAdd(&S.thist[p - 1][uint32_t(v) & 255u], uint32_t(hi - lo));
+        const uint32_t sh = 8u * p, v0 = a0 >> sh, v1 = last >> sh;
+        if (v0 == v1) {
+            atomicAdd(&S.thist[p - 1][v0 & 255u], w);
+        } else {
+            atomicAdd(&S.thist[p - 1][v0 & 255u], ((v0 + 1u) << sh) - a0);
+            for (uint32_t v = v0 + 1u; v < v1; ++v) atomicAdd(&S.thist[p - 1][v & 255u], 1u << sh);
+            atomicAdd(&S.thist[p - 1][v1 & 255u], last - (v1 << sh) + 1u);
         }
     }
 }
@@ -325,6 +331,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
         const uint32_t e = (tid < cnt && a.ent_idx) ? a.ent_idx[i] : 0u;
         for (uint32_t v = 0; v < a.n_views; ++v) {
             Splat sp;
+            uint4 rect = make_uint4(0u, 0u, 0u, 0u);
             uint32_t tiles = 0;
             if (tid < cnt && staged) {
                 const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
@@ -332,7 +339,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
 #pragma unroll
                 for (int k = 0; k < kEntityMatFloats; ++k) emr[k] = __ldg(em + k);
                 tiles = project_one(Rec{S.rec[stage] + tid * kRecordFloats}, emr, a.views[v], a.sh_degree,
-                                    a.band3_compat != 0, sp);
+                                    a.band3_compat != 0, sp, rect);
             } else {
                 sp = Splat{0.f, 0.f, 0.f, 0u, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             }
@@ -357,14 +364,11 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
                     }
                 }
                 if (tiles && ndig) {
-                    // the keys this item will emit: its tile rectangle as key
-                    // duplication computes it from the stored splat
+                    // the keys this item will emit: the tile ids of its rectangle
                     const ViewConst& vc = a.views[v];
                     const uint32_t gx = grid_x(vc.width);
-                    uint32_t x0, y0, x1, y1;
-                    bounding_rect(sp.px, sp.py, sp.radius, gx, grid_y(vc.height), x0, y0, x1, y1);
-                    if (sp.radius > 0.0f && x1 > x0 && y1 > y0)
-                        for (uint32_t y = y0; y < y1; ++y) count_tile_row(S, vc.tile_base + y * gx + x0, x1 - x0, ndig);
+                    for (uint32_t y = rect.y; y < rect.w; ++y)
+                        count_tile_row(S, vc.tile_base + y * gx + rect.x, rect.z - rect.x, ndig);
                 }
             }
         }
