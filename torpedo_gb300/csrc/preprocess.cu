@@ -290,7 +290,8 @@ __device__ __forceinline__ void count_tile_row(PreSmem& S, uint32_t a0, uint32_t
     }
 }
 
-__global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs a) {
+// (3 CTAs per SM fit in shared memory: registers up to 170 per thread are free)
+__global__ void __launch_bounds__(kPreThreads, 3) preprocess_kernel(PreprocessArgs a) {
     extern __shared__ __align__(128) unsigned char pre_smem[];
     PreSmem& S = *reinterpret_cast<PreSmem*>(pre_smem);
 
@@ -363,12 +364,32 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(PreprocessArgs 
                         }
                     }
                 }
-                if (tiles && ndig) {
-                    // the keys this item will emit: the tile ids of its rectangle
+            }
+            if (ndig) {
+                // the keys the warp's items will emit, the tile ids of their
+                // rectangles: the rows of all 32 rectangles are spread over the
+                // lanes (row r goes to lane r % 32, which finds the rectangle
+                // holding it by a binary search over the warp's row prefix)
+                const uint32_t lane = tid & 31u;
+                const uint32_t h = tiles ? rect.w - rect.y : 0u;
+                const uint32_t incl = warp_inclusive_scan(h);
+                const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                if (total) {
                     const ViewConst& vc = a.views[v];
                     const uint32_t gx = grid_x(vc.width);
-                    for (uint32_t y = rect.y; y < rect.w; ++y)
-                        count_tile_row(S, vc.tile_base + y * gx + rect.x, rect.z - rect.x, ndig);
+                    const uint32_t row0 = vc.tile_base + rect.y * gx + rect.x, w = rect.z - rect.x, excl = incl - h;
+                    for (uint32_t r0 = 0; r0 < total; r0 += 32u) {
+                        const uint32_t r = r0 + lane;
+                        uint32_t own = 0;  // lanes whose rows all come before row r
+#pragma unroll
+                        for (uint32_t step = 16; step; step >>= 1)
+                            if (__shfl_sync(0xFFFFFFFFu, incl, own + step - 1u) <= r) own += step;
+                        own = min(own, 31u);
+                        const uint32_t o_row0 = __shfl_sync(0xFFFFFFFFu, row0, own);
+                        const uint32_t o_w = __shfl_sync(0xFFFFFFFFu, w, own);
+                        const uint32_t o_excl = __shfl_sync(0xFFFFFFFFu, excl, own);
+                        if (r < total) count_tile_row(S, o_row0 + (r - o_excl) * gx, o_w, ndig);
+                    }
                 }
             }
         }
