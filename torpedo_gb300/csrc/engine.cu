@@ -6,9 +6,10 @@
 //  - The reference reads tilesRendered back to the host in the middle of every
 //    frame (GaussianEngine.cpp:665-674) to size its key buffers. Here every
 //    kernel after the scan reads K from device memory and the key buffers have
-//    a capacity: keygen drops keys past it and raises a status bit, and the
-//    host grows the buffers and re-runs the frame. A frame therefore has no
-//    host round trip and is replayed as one CUDA graph.
+//    a capacity: keygen drops keys past it and raises a status bit, the key
+//    sort and the blend then do nothing, and the host grows the buffers and
+//    re-runs the frame. A frame therefore has no host round trip and is
+//    replayed as one CUDA graph.
 //  - One stream, no queue-ownership transfers; images stay in device memory
 //    until tpd_read_image (the reference copies into a swapchain image).
 //  - Host waits poll an event with a time limit (the reference waits on

@@ -10,7 +10,9 @@
 // memory; threads then read their record with conflict-free 16-byte loads
 // (record stride 60 words). Besides the splat, each (view, Gaussian) gets a
 // depth-sort key (view << 32 | bits(viewZ)) whose digit histograms are
-// accumulated here. The tile counts are scanned afterwards in depth order
+// accumulated here, and the digits of the tile ids its keys will carry are
+// counted from its tile rectangle for the key sort (count_tile_row). The tile
+// counts are scanned afterwards in depth order
 // (scan_tiles_kernel<true>: gather + decoupled look-back, partitions by atomic
 // ticket). Arithmetic follows the shader source left to right with matrix
 // products accumulated k = 0..n-1; this file is compiled with --fmad=false so

@@ -1,4 +1,4 @@
-// sort.cu — kernel (c): stable LSD radix sort of (u64 key, u32 value) pairs.
+// sort.cu — kernel (c): stable LSD radix sort of (u64 or u32 key, u32 value) pairs.
 //
 // Reference: the 4-way (2-bit digit) LSD sort of radix-shuffle.slang:39-151,
 // radix-prefixA.slang:39-170, radix-prefixB.slang:39-169 and
@@ -8,18 +8,22 @@
 //
 // GB300 form (onesweep): 8-bit digits, so a 45-bit (tile | depth) key takes 6
 // passes instead of 23.
-//  1. The digit histograms of all passes come from key duplication (keygen.cu)
-//     in the pipeline; sort_histogram_kernel builds them for standalone sorts
-//     (one read of the keys, warp match-any aggregation into shared memory,
-//     one global atomic per bin per CTA).
+//  1. In the frame the digit histograms come from earlier kernels: the
+//     preprocess counts the depth keys' digits and the tile ids' digits (from
+//     each Gaussian's tile rectangle); sort_histogram_kernel builds them for
+//     standalone sorts (one read of the keys, warp match-any aggregation into
+//     shared memory, one global atomic per bin per CTA).
 //  2. onesweep_kernel, once per pass: a persistent CTA takes 4096-key
 //     partitions by atomic ticket, loads them with coalesced warp-striped
-//     loads, ranks keys per warp (match-any, stable within the warp-striped
-//     order), combines warps per digit, publishes its digit counts, reorders
-//     the partition in shared memory while predecessors publish, resolves
-//     each digit's global prefix by a decoupled look-back (one thread per
-//     digit, four predecessors per round trip, bounded spin) and writes digit
-//     runs out coalesced.
+//     loads, ranks keys per warp (bit ballots, or match-any in the 512-thread
+//     variant; stable within the warp-striped order), combines warps per
+//     digit, publishes its digit counts, reorders the partition in shared
+//     memory while predecessors publish, resolves each digit's global prefix
+//     by a decoupled look-back (one thread per digit, four predecessors per
+//     round trip, bounded spin) and writes digit runs out coalesced.
+// In the frame the depth presort sorts 64-bit (view | depth) keys and the key
+// sort 32-bit tile ids (their depth order is already fixed); the standalone
+// sort takes 64-bit keys.
 // The result is the stable sort of the pairs by the low key_bits bits, the
 // same permutation as the reference's sort.
 #include <algorithm>
