@@ -131,3 +131,18 @@ def thin_rotated():
         recs.append(record(pos, op, tuple(float(s) for s in scale), quat=tuple(float(v) for v in q),
                            sh=rgb2sh(*(float(c) for c in rng.uniform(0, 1, 3)))))
     return np.stack(recs), camera()
+
+
+def wide_row():
+    """A 4200x48 view (263 x 3 tiles) with one large Gaussian just in front of
+    the camera whose tile rectangle spans every column, plus small ones along
+    the row: rows of more than 256 consecutive tile ids, where the low tile-id
+    digit wraps round all 256 values."""
+    cam = camera(4200, 48)
+    recs = [record((0.0, 0.0, -4.7), 0.6, (8.0, 0.4, 0.2), sh=rgb2sh(0.8, 0.3, 0.1))]
+    rng = np.random.default_rng(14)
+    for _ in range(60):
+        recs.append(record((float(rng.uniform(-40, 40)), float(rng.uniform(-0.1, 0.1)), float(rng.uniform(-1, 1))),
+                           float(rng.uniform(0.3, 0.9)), tuple(float(v) for v in rng.uniform(0.02, 0.1, 3)),
+                           sh=rgb2sh(*(float(c) for c in rng.uniform(0, 1, 3)))))
+    return np.stack(recs), cam

@@ -44,11 +44,13 @@ def _scene(name):
         return kat.screen_filling()
     if name == "kat_tiny_view":
         return kat.tiny_view()
+    if name == "kat_wide_row":
+        return kat.wide_row()
     raise KeyError(name)
 
 
 SCENES = ["cfg0", "cfg1_200k", "cfg2_50k", "odd_size", "kat_single", "kat_two", "kat_edge", "kat_culled",
-          "kat_screen_filling", "kat_tiny_view"]
+          "kat_screen_filling", "kat_tiny_view", "kat_wide_row"]
 _cache = {}
 
 
