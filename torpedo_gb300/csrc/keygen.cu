@@ -70,19 +70,40 @@ __global__ void __launch_bounds__(kKeygenThreads)
     uint32_t* owner = S.owner[warp];
     const uint32_t nwarps = (count + 31) / 32;
 
+    // The item index, key offset and splat texel (px, py, viewZ, radius) of a
+    // warp's next 32 items are loaded while it writes the keys of the current
+    // ones: the texel is a gather in depth order.
+    auto load_index = [&](uint32_t wi_, uint32_t& item, uint32_t& off) {
+        const uint32_t r = wi_ * 32u + lane;
+        item = 0xFFFFFFFFu;
+        off = 0;
+        if (wi_ < nwarps && r < count) {
+            item = items[r];
+            off = offsets[r];
+        }
+    };
+    auto load_texel = [&](uint32_t item) {
+        return item < n_items ? reinterpret_cast<const float4*>(splats + item)[1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    uint32_t item_c, off_c;
+    load_index(warp_global, item_c, off_c);
+    float4 texel_c = load_texel(item_c);
+
     for (uint32_t wi = warp_global; wi < nwarps; wi += warps_total) {
+        uint32_t item_n, off_n;
+        load_index(wi + warps_total, item_n, off_n);
         const uint32_t r = wi * 32u + lane;
         // per item: first tile (row-major in its view), rect width and height, view grid width
         uint32_t w = 1, h = 0, gx = 1, off = 0, gi = 0, t0 = 0;
         if (r < count) {
-            const uint32_t item = items[r];
-            off = offsets[r];
+            const uint32_t item = item_c;
+            off = off_c;
             if (TPD_INBOUNDS(ctl, 21, item, n_items)) {
                 const uint32_t v = n_items == n ? 0u : item / n;  // one view: no division
                 gi = item - v * n;
                 const ViewConst& vc = views[v];
                 gx = grid_x(vc.width);
-                const float4 texel = reinterpret_cast<const float4*>(splats + item)[1];  // px, py, viewZ, radius
+                const float4 texel = texel_c;
                 if (texel.w > 0.0f) {
                     uint32_t x0, y0, x1, y1;
                     bounding_rect(texel.x, texel.y, texel.w, gx, grid_y(vc.height), x0, y0, x1, y1);
@@ -103,6 +124,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
         S.wgx[warp][lane] = w | (gx << 16);
         S.excl[warp][lane] = excl;
         S.gi[warp][lane] = gi;
+        const float4 texel_n = load_texel(item_n);
 
         for (uint32_t c0 = 0; c0 < total; c0 += kKeyWindow) {
             const uint32_t span = min(kKeyWindow, total - c0);
@@ -159,6 +181,9 @@ __global__ void __launch_bounds__(kKeygenThreads)
             __syncwarp();  // the owner map is rebuilt for the next window
         }
         __syncwarp();  // the lane table is rewritten by the next items
+        item_c = item_n;
+        off_c = off_n;
+        texel_c = texel_n;
     }
 }
 
