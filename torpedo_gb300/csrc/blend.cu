@@ -129,9 +129,10 @@ __device__ __forceinline__ float ex2_approx(float x) {
 // true when the pair is skipped (power > 0 or alpha < 1/255)
 __device__ __forceinline__ bool pair_skipped(float p2, float thr) { return p2 > 0.0f || p2 < thr; }
 
-__device__ __forceinline__ void load_view_tile(const BlendArgs* /*unused*/, const ViewConst* views,
-                                               const uint32_t* tile_view, uint32_t tile, uint32_t& vi,
-                                               uint32_t& width, uint32_t& height, uint32_t& tx, uint32_t& ty) {
+// View of a global tile id, that view's size, and the tile's (column, row) in it.
+__device__ __forceinline__ void load_view_tile(const ViewConst* views, const uint32_t* tile_view, uint32_t tile,
+                                               uint32_t& vi, uint32_t& width, uint32_t& height, uint32_t& tx,
+                                               uint32_t& ty) {
     vi = tile_view ? tile_view[tile] : 0u;
     const ViewConst& v = views[vi];
     width = v.width;
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdMinBlocks) blend_kernel(Blend
     // an overflowed frame is re-rendered with larger key buffers; nothing to draw
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
     uint32_t vi, W, H, tx, ty;
-    load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
+    load_view_tile(a.views, a.tile_view, tile, vi, W, H, tx, ty);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t px = tx * kBlockX + 8u * (warp & 1u) + (lane & 7u);
     const uint32_t pya = ty * kBlockY + 8u * (warp >> 1) + (lane >> 3), pyb = pya + 4u;
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(kFwdThreads, kBwdMinBlocks) blend_backward_ker
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
     if (!TPD_INBOUNDS(a.ctl, 44, tile, a.n_tiles)) return;
     uint32_t vi, W, H, tx, ty;
-    load_view_tile(nullptr, a.views, a.tile_view, tile, vi, W, H, tx, ty);
+    load_view_tile(a.views, a.tile_view, tile, vi, W, H, tx, ty);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t px = tx * kBlockX + 8u * (warp & 1u) + (lane & 7u);
     const uint32_t pya = ty * kBlockY + 8u * (warp >> 1) + (lane >> 3), pyb = pya + 4u;
