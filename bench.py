@@ -5,7 +5,9 @@ A step is one forward frame: preprocess -> tile-count scan -> key duplication ->
 radix sort -> tile ranges -> blend, with the Gaussians resident in device memory.
 
   value  frames/s over --steps frames enqueued back to back (CUDA graph replay),
-         CUDA events on the engine's stream, max over ranks
+         CUDA events on the engine's stream, max over ranks; the timed region
+         of --steps frames runs 5 times and value is the median region
+         (timed_regions_ms lists all five)
   e2e    frames/s through the C ABI with host buffers: per step the camera is
          uploaded from pinned host memory, the frame rendered and the RGBA8 image
          read back into pinned host memory (tpd_render_async / tpd_wait_render,
@@ -21,7 +23,11 @@ radix sort -> tile ranges -> blend, with the Gaussians resident in device memory
          backward as one captured graph per step (tpd_step_async)
   batched  views/s on cfg3 (500,000 Gaussians, 64 views of mixed sizes):
          forward + backward of all 64 views as one graph per step, against
-         the plain pipeline rendering and differentiating one view per call
+         the plain pipeline rendering and differentiating one view per call;
+         stages_ms splits the step by stage
+  large  views/s on cfg4 (6,000,000 Gaussians, 8 views of 3840x2160),
+         forward + backward per step, with the key count and the device
+         memory the engine holds
   autotune  the launch setting picked for the workload (torpedo_gb300.autotune)
          and the per-frame time of each candidate
 
@@ -46,6 +52,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "fwd FPS at 1M Gaussians 1080p (cfg1); sort GB/s vs HBM in roofline"
 UNIT = "frames/s"
+REGIONS = 5  # timed regions of --steps frames each; value is their median
+FRAME_STAGES = ("preprocess", "depth_sort", "keygen", "key_sort", "ranges", "blend")
 
 
 def peaks():
@@ -115,11 +123,11 @@ def dist_setup():
     return world, rank, local
 
 
-def cpu_frames(records, cam, budget_s: float, threads: int, max_frames: int):
-    """Times the oracle's FP32 transcription on whole frames until the budget is spent."""
+def cpu_frames(records, oc, budget_s: float, threads: int, max_frames: int):
+    """Times the oracle's FP32 transcription on whole frames (camera constants
+    oc, an oracle camera) until the budget is spent."""
     from oracle import oracle as O
 
-    oc = O.camera(cam.view, cam.projview(), cam.width, cam.height, focal=(cam.proj[0, 0], cam.proj[1, 1]))
     times = []
     k = 0
     t_all = time.perf_counter()
@@ -132,34 +140,45 @@ def cpu_frames(records, cam, budget_s: float, threads: int, max_frames: int):
     return times, k
 
 
+def oracle_workload(cfg_name: str):
+    """Records and camera constants of a one-view workload built by the oracle
+    alone (its own seeded generator and camera maths, equal bit for bit to the
+    product's): the reference arm loads nothing of the product library."""
+    from oracle import oracle as O
+    from torpedo_gb300.configs import CONFIGS, FAR, FOV, NEAR, UP
+
+    cfg = CONFIGS[cfg_name]
+    if cfg.views != 1:
+        raise SystemExit(f"--impl reference times one-view workloads; {cfg_name} has {cfg.views} views")
+    w, h = cfg.sizes[0]
+    recs = O.synthetic_records(int(cfg.name[3:]), cfg.n, cfg.mean_box)
+    return cfg, recs, O.orbit_camera((0.0, 0.0, -5.0), w, h, FOV, NEAR, FAR, UP)
+
+
 def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
         return
-    from torpedo_gb300 import configs
-
-    cfg = configs.CONFIGS[args.config]
-    sc = configs.scene(cfg)
-    cam = configs.cameras(cfg)[0]
+    cfg, recs, oc = oracle_workload(args.config)
     threads = os.cpu_count() or 1
     # warm-up frames, then timed frames; the run is capped at ~3 minutes of CPU time
-    per_frame = cpu_frames(sc.records, cam, 0.0, threads, 1)[0][0]
+    per_frame = cpu_frames(recs, oc, 0.0, threads, 1)[0][0]
     warm = max(0, min(args.warmup, int(20 / max(per_frame, 1e-3))))
     if warm:
-        cpu_frames(sc.records, cam, 1e9, threads, warm)
+        cpu_frames(recs, oc, 1e9, threads, warm)
     steps = max(3, min(args.steps, int(150 / max(per_frame, 1e-3))))
-    times, k = cpu_frames(sc.records, cam, 1e9, threads, steps)
+    times, k = cpu_frames(recs, oc, 1e9, threads, steps)
     total = sum(times)
     value = len(times) / total
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": len(times), "warmup": warm, "ms_per_step": round(1000 * total / len(times), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(cfg, cam, k),
+        "config": workload_config(cfg, oc.width, oc.height, k),
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(times)} whole {cfg.name} frames of the FP32 transcription of the "
-                                   f"reference shaders (4-way radix sort, {ref_passes(cam)} passes over K={k} "
-                                   f"keys), OpenMP over workgroups"},
+                                   f"reference shaders (4-way radix sort, {ref_passes(oc.width, oc.height)} passes "
+                                   f"over K={k} keys), OpenMP over workgroups"},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's Vulkan/Slang path cannot run here (no Vulkan, no slangc, no software renderer); "
                 "this arm times the oracle's line-by-line FP32 transcription of its shaders",
@@ -167,16 +186,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def ref_passes(cam) -> int:
+def ref_passes(width: int, height: int) -> int:
     from oracle import oracle as O
 
-    return O.radix_pass_count(cam.width, cam.height)
+    return O.radix_pass_count(width, height)
 
 
-def workload_config(cfg, cam, keys):
-    return {"workload": f"{cfg.name}: {cfg.n:,} Gaussians, {cam.width}x{cam.height}, SH degree 3, 16x16 tiles, "
+def workload_config(cfg, width, height, keys):
+    return {"workload": f"{cfg.name}: {cfg.n:,} Gaussians, {width}x{height}, SH degree 3, 16x16 tiles, "
                         f"means U[-{cfg.mean_box:g},{cfg.mean_box:g}]^3, camera (0,0,-5) fov 60",
-            "n_gaussians": cfg.n, "image": [cam.width, cam.height], "keys": int(keys), "views": 1,
+            "n_gaussians": cfg.n, "image": [width, height], "keys": int(keys), "views": 1,
             "l2": "inputs larger than L2: 240 MB of records and >= 100 MB of keys per frame",
             "parallelism": "replicas"}
 
@@ -237,9 +256,12 @@ def _params(sc, dev):
             (sc.means, sc.log_scales, sc.quats, sc.opacity_logits, sc.sh)]
 
 
-def train_rate(cfg_name, stream, local, steps, warmup, settings):
+def train_rate(cfg_name, stream, local, steps, warmup, settings, stage_steps=0):
     """Forward + backward steps (one captured graph each) on every view of a
-    config at once; returns (ms per step, stats, views, pixels)."""
+    config at once; returns (ms per step, stats, views, pixels, stages, extra):
+    with stage_steps > 0 also the per-stage ms of a step (another engine with
+    stage timing runs that many steps eagerly, CUDA events between stages),
+    and the device memory the engine holds (cudaMemGetInfo before and after)."""
     import torch
 
     import torpedo_gb300 as T
@@ -250,21 +272,29 @@ def train_rate(cfg_name, stream, local, steps, warmup, settings):
     sc = configs.scene(cfg)
     cams = configs.cameras(cfg)
     params = _params(sc, dev)
-    eng = T.GaussianEngine(device=local, stream=stream.cuda_stream, **settings)
-    try:
-        eng.compile_params(*params)
+    pixels = sum(c.width * c.height for c in cams)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(cfg.name[3:]))
+    dimg = torch.randn(pixels * 3, generator=gen, device=dev)
+    grads = [torch.empty_like(p) for p in params]
+    torch.cuda.synchronize(dev)
+    free0 = torch.cuda.mem_get_info(dev)[0]
+
+    def engine(**extra):
+        e = T.GaussianEngine(device=local, stream=stream.cuda_stream, **settings, **extra)
+        e.compile_params(*params)
         if len(cams) == 1:
-            eng.set_camera(cams[0])
+            e.set_camera(cams[0])
         else:
-            eng.set_views(cams)
-        eng.raster_frame()
-        pixels = sum(c.width * c.height for c in cams)
-        gen = torch.Generator(device=dev)
-        gen.manual_seed(int(cfg.name[3:]))
-        dimg = torch.randn(pixels * 3, generator=gen, device=dev)
-        grads = [torch.empty_like(p) for p in params]
+            e.set_views(cams)
+        e.raster_frame()
+        return e
+
+    eng = engine()
+    try:
         eng.step_async(dimg, grads, max(3, warmup))
         eng.sync()
+        held = free0 - torch.cuda.mem_get_info(dev)[0]
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         eng.step_async(dimg, grads, steps)
@@ -273,7 +303,20 @@ def train_rate(cfg_name, stream, local, steps, warmup, settings):
         ms = a.elapsed_time(b) / steps
     finally:
         eng.close()
-    return ms, st, len(cams), pixels
+    stages = None
+    if stage_steps:
+        eng = engine(stage_timing=True)
+        try:
+            eng.step_async(dimg, grads, 1)
+            eng.sync()
+            eng.stage_times(reset=True)
+            eng.step_async(dimg, grads, stage_steps)
+            eng.sync()
+            tot, nfr = eng.stage_times()
+            stages = {k: round(v / max(1, nfr), 4) for k, v in tot.items() if k != "ranges"}
+        finally:
+            eng.close()
+    return ms, st, len(cams), pixels, stages, {"device_bytes_held": int(held)}
 
 
 def plain_views_rate(cfg_name, local, passes, settings):
@@ -332,7 +375,7 @@ def run_train_only(args):
     stream = torch.cuda.Stream(torch.device("cuda", 0))
     settings = {"sort_ctas_per_sm": args.sort_ctas or 2, "sort_threads": args.sort_threads or 512,
                 "depth_sort_items": args.depth_sort_items or 16, "depth_sort_threads": args.depth_sort_threads or 256}
-    ms, st, _, _ = train_rate("cfg2", stream, 0, args.steps, args.warmup, settings)
+    ms, st, _, _, _, _ = train_rate("cfg2", stream, 0, args.steps, args.warmup, settings)
     print(json.dumps({"fwd_bwd": {"config": "cfg2", "value": round(1000.0 / ms, 3), "unit": "it/s",
                                   "ms_per_step": round(ms, 4), "keys": int(st["keys"]), "settings": settings}}))
 
@@ -399,16 +442,21 @@ def run_ours(args):
     barrier()
     clocks.start()
     time.sleep(0.3)
-    # timed region: value
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    e0.record(stream)
-    eng.raster_frames_async(args.steps)
-    e1.record(stream)
-    st = eng.sync()
-    barrier()
-    ms = max_over_ranks(e0.elapsed_time(e1))
+    # timed regions: value is the median of REGIONS regions of exactly
+    # args.steps frames each, every region bracketed by barrier + synchronize
+    # and timed with CUDA events on the engine's stream, max over ranks
+    region_ms = []
+    for _ in range(REGIONS):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        eng.raster_frames_async(args.steps)
+        e1.record(stream)
+        st = eng.sync()
+        barrier()
+        region_ms.append(max_over_ranks(e0.elapsed_time(e1)))
     clk = clocks.stop()
+    ms = sorted(region_ms)[len(region_ms) // 2]
     value = world * args.steps / (ms / 1000.0)
 
     # stage-timed region: live per-stage durations for the roofline
@@ -419,7 +467,7 @@ def run_ours(args):
     eng_t.sync()
     stage_ms, nfr = eng_t.stage_times()
     eng_t.close()
-    stage_avg = {k: v / max(1, nfr) for k, v in stage_ms.items()}
+    stage_avg = {k: v / max(1, nfr) for k, v in stage_ms.items() if k in FRAME_STAGES}
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -476,15 +524,15 @@ def run_ours(args):
                      "peak_tflops": round(fp32_peak, 1), "frac": round(pairs_s * 20 / 1e12 / fp32_peak, 4),
                      "note": "20 FP32 operations per evaluated pair; peak = SMs x 128 FP32 lanes x 2 x max SM clock"}
 
-    fwd_bwd = batched = None
+    fwd_bwd = batched = large = None
     if not args.no_train:
-        ms2, st2, _, _ = train_rate("cfg2", stream, local, 50, 3, settings)
+        ms2, st2, _, _, _, _ = train_rate("cfg2", stream, local, 50, 3, settings)
         fwd_bwd = {"config": "cfg2: 200,000 Gaussians (means N(0,1)^3), one 800x800 view, dL/dimage ~ N(0,1)",
                    "value": round(1000.0 / ms2, 3), "unit": "it/s", "ms_per_step": round(ms2, 4),
                    "keys": int(st2["keys"]),
                    "step": "forward frame + backward to means, log-scales, quaternions, opacity logits, SH; "
                            "one captured CUDA graph per step"}
-        ms3, st3, views3, pixels3 = train_rate("cfg3", stream, local, 5, 2, settings)
+        ms3, st3, views3, pixels3, stages3, _ = train_rate("cfg3", stream, local, 5, 2, settings, stage_steps=2)
         plain = plain_views_rate("cfg3", local, 3, settings)
         batched = {"config": "cfg3: 500,000 Gaussians (means N(0,1)^3), 64 views on a sphere of radius 5, sizes "
                              "from {640x480, 1280x720, 1920x1080} (seed 3), dL/dimage ~ N(0,1)",
@@ -492,13 +540,23 @@ def run_ours(args):
                    "keys": int(st3["keys"]), "pixels": pixels3,
                    "plain_views_per_s": round(plain, 2), "batched_over_plain": round(views3 * 1000.0 / ms3 / plain, 3),
                    "plain": "one view per call: set_camera, raster_frame, backward, each waiting for its work; "
-                            "fastest of 3 passes over the 64 views"}
+                            "fastest of 3 passes over the 64 views",
+                   "stages_ms": stages3,
+                   "stages_note": "per step, from 2 eager steps with CUDA events between stages (no graph)"}
+        if not args.no_large:
+            ms4, st4, views4, pixels4, _, ex4 = train_rate("cfg4", stream, local, 3, 1, settings)
+            large = {"config": "cfg4: 6,000,000 Gaussians (means U[-10,10]^3), 8 views of 3840x2160, "
+                               "dL/dimage ~ N(0,1)",
+                     "views_per_s": round(views4 * 1000.0 / ms4, 2), "ms_per_step": round(ms4, 3),
+                     "keys": int(st4["keys"]), "key_capacity": int(st4["key_capacity"]), "pixels": pixels4,
+                     "device_bytes_held": ex4["device_bytes_held"],
+                     "step": "forward + backward of the 8 views as one captured graph per step"}
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded cfg1 generator)",
-        "config": workload_config(cfg, cam, K),
+        "config": workload_config(cfg, cam.width, cam.height, K),
         "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit tile-id radix pass of the key sort)",
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_kind": f"{peak_kind} copy bandwidth",
@@ -526,12 +584,17 @@ def run_ours(args):
         "autotune": {"settings": settings, "ms_per_frame": tuned},
         "fwd_bwd": fwd_bwd,
         "batched": batched,
+        "large": large,
+        "timed_regions_ms": [round(x, 4) for x in region_ms],
     }
     if e2e:
         line["e2e"] = e2e
     if rank == 0 and world == 1 and args.cpu_baseline_s > 0:
+        from oracle import oracle as O
+
         threads = os.cpu_count() or 1
-        times, k = cpu_frames(sc.records, cam, args.cpu_baseline_s, threads, 50)
+        oc = O.camera(cam.view, cam.projview(), cam.width, cam.height, focal=(cam.proj[0, 0], cam.proj[1, 1]))
+        times, k = cpu_frames(sc.records, oc, args.cpu_baseline_s, threads, 50)
         line["cpu_baseline"] = {"value": round(len(times) / sum(times), 4), "unit": UNIT, "cores": threads,
                                 "kind": "port",
                                 "sample": f"{len(times)} whole frames of the FP32 transcription of the reference "
@@ -557,7 +620,8 @@ def main():
     ap.add_argument("--sort-threads", type=int, default=0, help="with --sort-ctas: radix CTA size (256 or 512)")
     ap.add_argument("--depth-sort-items", type=int, default=0, help="with --sort-ctas: depth sort keys per thread")
     ap.add_argument("--depth-sort-threads", type=int, default=0, help="with --sort-ctas: depth sort CTA size (256 or 512)")
-    ap.add_argument("--no-train", action="store_true", help="skip the cfg2 and cfg3 forward+backward measurements")
+    ap.add_argument("--no-train", action="store_true", help="skip the cfg2, cfg3 and cfg4 forward+backward measurements")
+    ap.add_argument("--no-large", action="store_true", help="skip the cfg4 forward+backward measurement")
     ap.add_argument("--train-only", action="store_true", help="only the cfg2 forward+backward steps (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -53,6 +53,13 @@ typedef enum tpd_status {
     TPD_ERR_IO = 7         /* file could not be read or parsed */
 } tpd_status;
 
+/* Device status bits: tpd_frame_stats.status, and the status word that the
+ * stage entry points leave in their scratch (see tpd_sort_pairs). 0 = clean. */
+#define TPD_DEVSTAT_KEY_OVERFLOW 0x1u      /* more keys than the key buffers hold (the frame is rendered again) */
+#define TPD_DEVSTAT_LOOKBACK_TIMEOUT 0x2u  /* a decoupled look-back wait ran out: prefixes and offsets are invalid */
+#define TPD_DEVSTAT_BAD_INPUT 0x8u         /* an input outside its documented range */
+#define TPD_DEVSTAT_BAD_INDEX 0x10u        /* an index failed its bounds check; the access was skipped */
+
 typedef struct tpd_engine tpd_engine;
 
 typedef struct tpd_settings {
@@ -74,7 +81,7 @@ typedef struct tpd_settings {
     uint32_t reserved[2];
 } tpd_settings;
 
-/* Stages of a frame, for tpd_stage_times. */
+/* Stages of a frame (and of a training step), for tpd_stage_times. */
 enum {
     TPD_STAGE_PREPROCESS = 0, /* camera upload, entity matrices, preprocess (splats + depth keys) */
     TPD_STAGE_DEPTH_SORT = 1, /* radix sort of the (view | depth) keys, tile-count scan in depth order */
@@ -82,7 +89,10 @@ enum {
     TPD_STAGE_KEY_SORT = 3,   /* radix sort of the (tile | depth) keys on their tile-id bits */
     TPD_STAGE_RANGES = 4,     /* empty: the key sort's last pass writes the tile ranges */
     TPD_STAGE_BLEND = 5,      /* alpha blend */
-    TPD_STAGE_COUNT = 6
+    TPD_STAGE_BACKWARD_SETUP = 6,      /* tpd_step_async: gradient clear and the adjoint's tile order (0 in frames) */
+    TPD_STAGE_BLEND_BACKWARD = 7,      /* tpd_step_async: blend adjoint (0 in frames) */
+    TPD_STAGE_PREPROCESS_BACKWARD = 8, /* tpd_step_async: preprocess adjoint (0 in frames) */
+    TPD_STAGE_COUNT = 9
 };
 
 typedef struct tpd_frame_stats {
@@ -216,14 +226,20 @@ TPD_API uint32_t tpd_key_bits_for_tiles(uint32_t tiles);
 /* Radix sort (radix-shuffle / prefixA / prefixB / mapping .slang): stable
  * sort of n (key, value) pairs on the low key_bits bits. Result in keys/vals
  * if *result_in_alt == 0, else in keys_alt/vals_alt. workspace: at least
- * tpd_sort_workspace_size(n) bytes of device memory. */
+ * tpd_sort_workspace_size(n) bytes of device memory, 16-byte aligned.
+ * The call enqueues its work on the stream and returns; once that work is
+ * done, the uint32 at byte offset TPD_WORKSPACE_STATUS_OFFSET of the
+ * workspace holds the device status (TPD_DEVSTAT_* bits): anything but 0
+ * means the result is invalid. */
+#define TPD_WORKSPACE_STATUS_OFFSET 0
 TPD_API size_t tpd_sort_workspace_size(uint32_t n);
 TPD_API int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t n,
                    uint32_t key_bits, void* workspace, size_t workspace_bytes, void* stream, int* result_in_alt);
 
 /* prefix.slang: exclusive scan of the tiles word of n 48-byte splats into
  * offsets (u32), total into *total (device u32). workspace: at least
- * tpd_scan_workspace_size(n) bytes of device memory. */
+ * tpd_scan_workspace_size(n) bytes of device memory, 16-byte aligned; its
+ * status word (TPD_WORKSPACE_STATUS_OFFSET) as for tpd_sort_pairs. */
 TPD_API size_t tpd_scan_workspace_size(uint32_t n);
 TPD_API int tpd_scan_tiles(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total, void* workspace,
                    size_t workspace_bytes, void* stream);
@@ -238,9 +254,20 @@ TPD_API int tpd_scan_tiles(const void* splats, uint32_t n, uint32_t* offsets, ui
  * up the scratch's address and should come before any stream capture. One
  * scratch per device: calls whose work overlaps on one device race, so order
  * them on one stream. Each call clears its scratch first; nothing has to
- * start at zero. */
+ * start at zero. The scratch address is looked up once per device in the
+ * device's primary context (the runtime's default): do not call it from
+ * another driver context, nor after cudaDeviceReset in the same process.
+ * status (nullable, device u32) receives the scan's device status
+ * (TPD_DEVSTAT_* bits) on the stream: anything but 0 means offsets and total
+ * are invalid. */
 #define TPD_SCAN_STATIC_MAX_SPLATS (1u << 24)
-TPD_API int tpd_scan_tiles_static(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total, void* stream);
+TPD_API int tpd_scan_tiles_static(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total,
+                                  uint32_t* status, void* stream);
+
+/* Test hook: nonzero makes partition 0 of every later tpd_scan_tiles /
+ * tpd_scan_tiles_static call never publish its look-back descriptor, so the
+ * bounded wait of partition 1 runs out and the call's status reports it. */
+TPD_API void tpd_test_set_never_publish(uint32_t on);
 
 /* ---- host utilities (no device) ---- */
 

@@ -13,7 +13,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 LIB = OUT / "liboracle.so"
-SOURCES = ["tpd_oracle.cpp", "tpd_oracle_bwd.cpp"]
+SOURCES = ["tpd_oracle.cpp", "tpd_oracle_bwd.cpp", "tpd_oracle_host.cpp"]
 
 
 def build(force: bool = False) -> Path:

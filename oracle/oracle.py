@@ -53,6 +53,10 @@ def load():
                                              C.c_int, P, P, P]),
             "orc_backward_f64": (None, [C.POINTER(OrcParams64), C.c_uint32, C.POINTER(OrcCamera), C.c_uint32, C.c_int,
                                         P, P, P, P, P, P, P, P, P]),
+            "orc_look_at": (None, [P, P, P, P]),
+            "orc_perspective": (None, [C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_float, P]),
+            "orc_mat4_mul": (None, [P, P, P]),
+            "orc_synthetic_scene": (None, [C.c_uint64, C.c_uint32, C.c_float, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -64,6 +68,43 @@ def load():
 
 def _c(a, dtype):
     return np.ascontiguousarray(np.asarray(a, dtype=dtype))
+
+
+def look_at(eye, center, up) -> np.ndarray:
+    """Camera::lookAt with the reference's accurate arithmetic: 4x4 row-major float32."""
+    e, c, u = (_c(v, np.float32).reshape(3) for v in (eye, center, up))
+    out = np.zeros((4, 4), np.float32)
+    load().orc_look_at(e.ctypes.data, c.ctypes.data, u.ctypes.data, out.ctypes.data)
+    return out
+
+
+def perspective(width: int, height: int, fov_y_degrees: float, near: float, far: float) -> np.ndarray:
+    """PerspectiveCamera's reversed-Z projection: 4x4 row-major float32."""
+    out = np.zeros((4, 4), np.float32)
+    load().orc_perspective(width, height, fov_y_degrees, near, far, out.ctypes.data)
+    return out
+
+
+def mat4_mul(a, b) -> np.ndarray:
+    """math::mul(a, b) with the reference's accurate dot product."""
+    a, b = _c(a, np.float32), _c(b, np.float32)
+    out = np.zeros((4, 4), np.float32)
+    load().orc_mat4_mul(a.ctypes.data, b.ctypes.data, out.ctypes.data)
+    return out
+
+
+def orbit_camera(eye, width: int, height: int, fov_y_degrees=60.0, near=0.2, far=100.0, up=(0.0, -1.0, 0.0)):
+    """Camera constants of a view at `eye` looking at the origin, as updateCameraBuffer packs them."""
+    view = look_at(eye, (0.0, 0.0, 0.0), up)
+    proj = perspective(width, height, fov_y_degrees, near, far)
+    return camera(view, mat4_mul(proj, view), width, height, focal=(proj[0, 0], proj[1, 1]))
+
+
+def synthetic_records(seed: int, n: int, mean_box: float = 0.0) -> np.ndarray:
+    """The seeded synthetic scene of the workloads as (n, 60) float32 records."""
+    rec = np.zeros((n, 60), np.float32)
+    load().orc_synthetic_scene(seed, n, float(mean_box), rec.ctypes.data)
+    return rec
 
 
 def camera(view, projview, width: int, height: int, focal=None) -> OrcCamera:

@@ -224,9 +224,10 @@ GOut<T> project_one(const GIn<T>& g, const T* model, const Cam<T>& cam, uint32_t
                       ((pp[1] + T(1.0)) * T(cam.H) - T(1.0)) * T(0.5)};
     // getBoundingRect (volume.slang:12-17) with getComputeGrid (common.slang:83-85)
     const uint32_t gx = (cam.W + BLOCK - 1) / BLOCK, gy = (cam.H + BLOCK - 1) / BLOCK;
-    const T bx = T(BLOCK), b1 = T(BLOCK - 1);
+    // p + r + BLOCK - 1: ((p + r) + 16) - 1, rounded after each operation as written
+    const T bx = T(BLOCK);
     const T v0 = (img[0] - radius) / bx, v1 = (img[1] - radius) / bx;
-    const T v2 = (img[0] + radius + b1) / bx, v3 = (img[1] + radius + b1) / bx;
+    const T v2 = (img[0] + radius + bx - T(1)) / bx, v3 = (img[1] + radius + bx - T(1)) / bx;
     auto clampi = [](int v, uint32_t g) -> uint32_t {
         int m = std::max(0, v);
         return std::min(g, (uint32_t)m);
@@ -350,7 +351,7 @@ void orc_keygen(const uint32_t* splats, const uint32_t* offsets, uint32_t n, uin
         if (radius <= 0.0f) continue;
         const float px = bitsf(s[4]), py = bitsf(s[5]);
         const float v0 = (px - radius) / 16.0f, v1 = (py - radius) / 16.0f;
-        const float v2 = (px + radius + 15.0f) / 16.0f, v3 = (py + radius + 15.0f) / 16.0f;
+        const float v2 = (px + radius + 16.0f - 1.0f) / 16.0f, v3 = (py + radius + 16.0f - 1.0f) / 16.0f;
         auto clampi = [](int v, uint32_t g) -> uint32_t { return std::min(g, (uint32_t)std::max(0, v)); };
         const uint32_t x0 = clampi(trunc_int(v0), gx), y0 = clampi(trunc_int(v1), gy);
         const uint32_t x1 = clampi(trunc_int(v2), gx), y1 = clampi(trunc_int(v3), gy);

@@ -116,6 +116,16 @@ void orc_blend_f64(const double* splat64, const uint32_t* vals, const uint32_t* 
 uint64_t orc_frame_f32(const float* recs, uint32_t n, const orc_camera* cam,
                        uint32_t sh_degree, float* image, int threads, uint32_t tile_rows_limit);
 
+/* ---- inputs (tpd_oracle_host.cpp): seeded scenes and camera matrices ----
+ * The camera maths of the reference (Camera::lookAt, PerspectiveCamera,
+ * math::mul) with its accurate dot / cross arithmetic; the seeded synthetic
+ * scene of the five workloads as 240-byte records. */
+void orc_look_at(const float eye[3], const float center[3], const float up[3], float view[16]);
+void orc_perspective(uint32_t width, uint32_t height, float fov_y_degrees, float near_plane, float far_plane,
+                     float proj[16]);
+void orc_mat4_mul(const float a[16], const float b[16], float out[16]);
+void orc_synthetic_scene(uint64_t seed, uint32_t n, float mean_box, float* records);
+
 /* ---- FP64 differentiable forward / backward over raw parameters ----
  * Raw parameters (double): means[n*3], log_scales[n*3], quats[n*4] (x,y,z,w,
  * used as stored, not normalised), opacity_logits[n], sh[n*48]; the scale

@@ -1,8 +1,8 @@
 """Generates the golden fixtures of tests/golden/ from the reference's own C++.
 
-Run in a checkout that has the reference tree (default /root/reference, or
-TPD_REFERENCE_ROOT): it builds oracle/_ref/libtpdref.so with oracle/build_ref.py
-and records
+Run where the reference tree is present (oracle/build_ref.py locates it; set
+TPD_REFERENCE_ROOT to point elsewhere): it builds oracle/_ref/libtpdref.so
+with oracle/build_ref.py and records
   reference_host.npz   camera matrices (view, projection, proj*view, focal) from
                        PerspectiveCamera + Camera::lookAt + math::mul, the
                        getHigherMSB table, and GaussianPoint::fromModel records

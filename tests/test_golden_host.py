@@ -32,6 +32,32 @@ def test_camera_matrices_bit_exact(gold):
         assert proj[0] == gold["cam_focal"][i][0] and proj[5] == gold["cam_focal"][i][1]
 
 
+def test_oracle_camera_matrices_bit_exact(gold):
+    """The oracle's own camera maths (it builds the reference arm's inputs
+    without the product library) against the same golden vectors."""
+    meta = gold["cam_meta"]
+    for i in range(meta.shape[0]):
+        eye, ctr, up = meta[i, 0:3], meta[i, 3:6], meta[i, 6:9]
+        w, h, fov, near, far = int(meta[i, 9]), int(meta[i, 10]), float(meta[i, 11]), float(meta[i, 12]), float(meta[i, 13])
+        view = O.look_at(eye, ctr, up).reshape(16)
+        proj = O.perspective(w, h, fov, near, far).reshape(16)
+        pv = O.mat4_mul(proj.reshape(4, 4), view.reshape(4, 4)).reshape(16)
+        np.testing.assert_array_equal(view.view(np.uint32), gold["cam_view"][i].view(np.uint32), err_msg=f"view {i}")
+        np.testing.assert_array_equal(proj.view(np.uint32), gold["cam_proj"][i].view(np.uint32), err_msg=f"proj {i}")
+        np.testing.assert_array_equal(pv.view(np.uint32), gold["cam_projview"][i].view(np.uint32), err_msg=f"pv {i}")
+    for a, b, ab in zip(gold["mul_a"], gold["mul_b"], gold["mul_ab"]):
+        np.testing.assert_array_equal(O.mat4_mul(a.reshape(4, 4), b.reshape(4, 4)).reshape(16).view(np.uint32),
+                                      ab.view(np.uint32))
+
+
+@pytest.mark.parametrize("seed,box", [(0, 0.0), (1, 3.0), (3, 0.0), (4, 10.0)])
+def test_oracle_scene_generator_equals_the_product_generator(seed, box):
+    """The seeded scene the oracle generates is the product's, byte for byte."""
+    a = O.synthetic_records(seed, 3000, box)
+    b = T.synthetic_scene(seed, 3000, box).records
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
 def test_mat4_mul_bit_exact(gold):
     for a, b, ab in zip(gold["mul_a"], gold["mul_b"], gold["mul_ab"]):
         np.testing.assert_array_equal(T.mat4_mul(a, b).reshape(16).view(np.uint32), ab.view(np.uint32))

@@ -12,7 +12,11 @@ _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libtpdsplat.so"
 
 TPD_OK, TPD_ERR_ARG, TPD_ERR_OOM, TPD_ERR_TIMEOUT, TPD_ERR_DEVICE, TPD_ERR_STATE, TPD_ERR_CAPACITY, TPD_ERR_IO = range(8)
 TPD_IMAGE_RGB32F, TPD_IMAGE_RGBA8 = 0, 1
-STAGES = ("preprocess", "depth_sort", "keygen", "key_sort", "ranges", "blend")
+STAGES = ("preprocess", "depth_sort", "keygen", "key_sort", "ranges", "blend", "backward_setup", "blend_backward",
+          "preprocess_backward")
+# device status bits (TPD_DEVSTAT_*) and the status word's offset in a stage workspace
+DEVSTAT_KEY_OVERFLOW, DEVSTAT_LOOKBACK_TIMEOUT, DEVSTAT_BAD_INPUT, DEVSTAT_BAD_INDEX = 0x1, 0x2, 0x8, 0x10
+WORKSPACE_STATUS_OFFSET = 0
 (TPD_BUF_RECORDS, TPD_BUF_SPLATS, TPD_BUF_OFFSETS, TPD_BUF_KEYS, TPD_BUF_VALUES, TPD_BUF_RANGES, TPD_BUF_IMAGE,
  TPD_BUF_FINAL_T, TPD_BUF_N_CONTRIB, TPD_BUF_G2D) = range(10)
 
@@ -93,7 +97,8 @@ SIGNATURES = {
     "tpd_sort_pairs": (C.c_int, [_P, _P, _P, _P, _U32, _U32, _P, C.c_size_t, _P, C.POINTER(C.c_int)]),
     "tpd_scan_workspace_size": (C.c_size_t, [_U32]),
     "tpd_scan_tiles": (C.c_int, [_P, _U32, _P, _P, _P, C.c_size_t, _P]),
-    "tpd_scan_tiles_static": (C.c_int, [_P, _U32, _P, _P, _P]),
+    "tpd_scan_tiles_static": (C.c_int, [_P, _U32, _P, _P, _P, _P]),
+    "tpd_test_set_never_publish": (None, [_U32]),
     "tpd_look_at": (None, [_F, _F, _F, _F]),
     "tpd_perspective": (None, [_U32, _U32, C.c_float, C.c_float, C.c_float, _F]),
     "tpd_mat4_mul": (None, [_F, _F, _F]),

@@ -590,14 +590,18 @@ void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStre
     pack_rgba8_kernel<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(rgb, rgba, pixels);
 }
 
+namespace {
+// more than 48 KB of shared memory needs the opt-in, on every device
+int blend_backward_setup() {
+    cudaFuncSetAttribute(blend_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(sizeof(BlendBackwardSmem)));
+    return 1;
+}
+}  // namespace
+
 void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s) {
     if (a.n_tiles == 0) return;
-    static bool configured = false;  // more than 48 KB of shared memory needs the opt-in
-    if (!configured) {
-        cudaFuncSetAttribute(blend_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(sizeof(BlendBackwardSmem)));
-        configured = true;
-    }
+    device_once(blend_backward_setup);
     blend_backward_kernel<<<a.n_tiles, kFwdThreads, sizeof(BlendBackwardSmem), s>>>(a);
 }
 

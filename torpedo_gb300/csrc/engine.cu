@@ -16,12 +16,16 @@
 //    fences with UINT64_MAX, GaussianEngine.cpp:634, 665).
 //  - V >= 1 views per frame; V = 1 reproduces the reference's keys exactly
 //    (tile ids without offset).
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/tpdsplat.h"
@@ -30,9 +34,37 @@
 
 using namespace tpd;
 
+namespace tpd {
+
+int device_once(int (*init)()) {
+    static std::mutex m;
+    static std::map<std::pair<int, uintptr_t>, int> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_pair(dev, reinterpret_cast<uintptr_t>(init));
+    std::lock_guard<std::mutex> lock(m);
+    const auto it = done.find(key);
+    if (it != done.end()) return it->second;
+    const int v = init();
+    done.emplace(key, v);
+    return v;
+}
+
+namespace {
+std::atomic<uint32_t> g_never_publish_standalone{0};
+}
+uint32_t test_never_publish_standalone() { return g_never_publish_standalone.load(); }
+
+}  // namespace tpd
+
 namespace {
 
 constexpr uint32_t kDefaultSpin = 1u << 20;
+// Look-back descriptors keep 30 bits of (frame tag * 32 + slot), so a tag
+// value comes round again after 2^25 frames; the engine clears its
+// descriptors whenever the frame tag reaches a multiple of this, and a stale
+// descriptor can then never carry the current frame's tag.
+constexpr uint64_t kTagWindow = 1ull << 25;
 constexpr uint32_t kScanTileStandalone = 1024;
 
 struct StatsHead {
@@ -119,6 +151,7 @@ struct tpd_engine {
     cudaEvent_t tev[kTimingSlots][kTimingEvents] = {};
     bool tev_pending[kTimingSlots] = {};
     int tslot = 0;
+    int cur_tslot = -1;  // the slot of the last enqueued frame (its backward stages are recorded there)
     double stage_ms[TPD_STAGE_COUNT] = {};
     uint64_t timed_frames = 0;
 
@@ -126,6 +159,7 @@ struct tpd_engine {
     bool graph_valid = false;
     bool needs_eager = true;  // the first frame after any change runs without a graph
     uint64_t frames = 0;
+    uint64_t tags = 0;  // frame tags issued so far (FrameCtl.tag of the last enqueued frame)
 
     // forward + backward step graph (tpd_step_async), keyed by the caller's pointers
     cudaGraphExec_t step_graph = nullptr;
@@ -294,6 +328,7 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
             for (int k = 0; k < tpd_engine::kTimingEvents; ++k) cudaEventCreate(&e->tev[slot][k]);
         ev = e->tev[slot];
         e->tev_pending[slot] = true;
+        e->cur_tslot = slot;
     }
     // TPD_DEBUG_SYNC=1 (eager frames only): synchronise after each stage and
     // name the first stage whose kernels report an error.
@@ -303,7 +338,8 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     }();
     cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(s, &cap_status);
-    static const char* kStageNames[] = {"begin", "preprocess", "depth sort", "keygen", "key sort", "ranges", "blend"};
+    static const char* kStageNames[] = {"begin", "preprocess", "depth sort", "keygen", "key sort", "ranges", "blend",
+                                        "backward set-up", "blend adjoint", "preprocess adjoint"};
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], s);
         if (debug_sync && cap_status == cudaStreamCaptureStatusNone) {
@@ -396,7 +432,21 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     ba.n_contrib = e->d_n_contrib;
     launch_blend(ba, s);
     mark(6);
+    // the backward stages of a frame without backward take no time; a
+    // training step records them again after its adjoint kernels
+    if (ev)
+        for (int k = TPD_STAGE_BACKWARD_SETUP + 1; k <= TPD_STAGE_PREPROCESS_BACKWARD + 1; ++k) cudaEventRecord(ev[k], s);
     if (io) cudaMemcpyAsync(e->h_stats, e->d_ctl, sizeof(StatsHead), cudaMemcpyDeviceToHost, s);
+}
+
+// Clears the look-back descriptors (stream-ordered) before the frame whose
+// tag reaches a multiple of kTagWindow; call once per frame launched, right
+// before it is enqueued or its graph launched.
+void before_frame(tpd_engine* e) {
+    if (++e->tags % kTagWindow != 0) return;
+    cudaMemsetAsync(e->d_desc_depth, 0, sort_desc_entries(uint32_t(e->splat_cap), 4) * 8, e->stream);
+    cudaMemsetAsync(e->d_desc_pre, 0, e->desc_pre_cap * 8, e->stream);
+    cudaMemsetAsync(e->d_desc_sort, 0, sort_desc_entries(uint32_t(e->capacity)) * 8, e->stream);
 }
 
 int run_frame_once(tpd_engine* e, bool use_graph) {
@@ -413,8 +463,10 @@ int run_frame_once(tpd_engine* e, bool use_graph) {
             e->graph = ge;
             e->graph_valid = true;
         }
+        before_frame(e);
         TPD_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
     } else {
+        before_frame(e);
         enqueue_frame(e);
         TPD_CUDA(e, cudaGetLastError());
     }
@@ -822,6 +874,7 @@ int tpd_raster_frames_async(tpd_engine* e, uint32_t count) {
         e->graph_valid = true;
     }
     for (uint32_t i = 0; i < count; ++i) {
+        before_frame(e);
         if (graph) TPD_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
         else enqueue_frame(e);
     }
@@ -884,8 +937,10 @@ int tpd_render_async(tpd_engine* e, void* dst, uint32_t format, int dst_is_devic
             TPD_CUDA(e, err);
             e->body_graph = ge;
         }
+        before_frame(e);
         TPD_CUDA(e, cudaGraphLaunch(e->body_graph, s));
     } else {
+        before_frame(e);
         enqueue_frame(e, false);
     }
     // image into the slot's staging buffer and stats into its pinned slot
@@ -991,6 +1046,13 @@ int prepare_backward(tpd_engine* e, BackwardOut& o) {
 
 // Blend adjoint (per-splat gradients, zeroed first) then preprocess adjoint.
 void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& o) {
+    // stage timing: the events of the frame this backward follows, while
+    // that frame's slot has not been harvested (tpd_step_async)
+    cudaEvent_t* ev = nullptr;
+    if (e->settings.stage_timing && e->cur_tslot >= 0 && e->tev_pending[e->cur_tslot]) ev = e->tev[e->cur_tslot];
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], e->stream);
+    };
     cudaMemsetAsync(e->d_g2d, 0, uint64_t(e->n) * e->n_views * kG2DStride * 4, e->stream);
     const int b = e->sorted_in_alt ? 1 : 0;
     BlendBackwardArgs bb{};
@@ -1012,7 +1074,9 @@ void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& 
     // longest tile lists first: the adjoint's cost per tile varies more than the forward's
     launch_tile_order(e->d_ranges, e->total_tiles, e->d_ctl, uint32_t(e->capacity), e->d_tile_order, e->stream);
     bb.tile_order = e->d_tile_order;
+    mark(TPD_STAGE_BACKWARD_SETUP + 1);
     launch_blend_backward(bb, e->stream);
+    mark(TPD_STAGE_BLEND_BACKWARD + 1);
     PreprocessBackwardArgs pb{};
     pb.recs = e->d_recs;
     pb.n = e->n;
@@ -1031,6 +1095,7 @@ void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& 
     pb.g_logits = o.logits;
     pb.g_sh = o.sh;
     launch_preprocess_backward(pb, e->stream);
+    mark(TPD_STAGE_PREPROCESS_BACKWARD + 1);
 }
 
 }  // namespace
@@ -1076,6 +1141,7 @@ int tpd_step_async(tpd_engine* e, const float* dL_dimage, float* g_means, float*
         std::memcpy(e->step_key, key, sizeof(key));
     }
     for (uint32_t i = 0; i < count; ++i) {
+        before_frame(e);
         if (graph) {
             TPD_CUDA(e, cudaGraphLaunch(e->step_graph, e->stream));
         } else {
@@ -1202,9 +1268,12 @@ int tpd_scan_tiles(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* 
     const size_t entries = size_t(n) / kScanTileStandalone + 2;
     if (cudaMemsetAsync(desc, 0, entries * 8, s) != cudaSuccess) return TPD_ERR_DEVICE;
     launch_sort_begin(ctl, 0, s);
-    launch_scan_tiles(static_cast<const Splat*>(splats), n, offsets, desc, ctl, kDefaultSpin, 0, s);
+    launch_scan_tiles(static_cast<const Splat*>(splats), n, offsets, desc, ctl, kDefaultSpin,
+                      test_never_publish_standalone(), s);
     if (cudaMemcpyAsync(total, &ctl->total_keys, 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TPD_ERR_DEVICE;
     return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;
 }
+
+void tpd_test_set_never_publish(uint32_t on) { g_never_publish_standalone.store(on ? 1u : 0u); }
 
 }  // extern "C"

@@ -187,6 +187,12 @@ __global__ void __launch_bounds__(kKeygenThreads)
     }
 }
 
+int keygen_setup() {
+    int r = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, keygen_kernel, kKeygenThreads, 0);
+    return r > 0 ? r : 1;
+}
+
 }  // namespace
 
 void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
@@ -195,12 +201,7 @@ void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* o
     if (n_items == 0 || n == 0) return;
     const uint64_t warps = (uint64_t(n_items) + 31) / 32;
     uint64_t blocks = (warps * 32 + kKeygenThreads - 1) / kKeygenThreads;
-    static int per_sm = 0;  // resident CTAs per SM (shared memory bound)
-    if (per_sm == 0) {
-        int r = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, keygen_kernel, kKeygenThreads, 0);
-        per_sm = r > 0 ? r : 1;
-    }
+    const int per_sm = device_once(keygen_setup);  // resident CTAs per SM (shared memory bound)
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
     blocks = blocks < cap ? blocks : cap;
     keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, n_items, n, views, tiles, vals,

@@ -6,9 +6,13 @@
 // covariance, EWA projection, Jacobian); prefix.slang:40-158 for the scan.
 //
 // GB300 layout: a CTA of 128 threads owns 128 consecutive records (30,720 B).
-// One elected thread stages them with a single TMA bulk copy into shared
-// memory; threads then read their record with conflict-free 16-byte loads
-// (record stride 60 words). Besides the splat, each (view, Gaussian) gets a
+// The CTA stages them into shared memory with coalesced 16-byte asynchronous
+// copies (cp.async, 15 per thread), double-buffered so the next chunk streams
+// in while this one is projected; threads then read their record with
+// conflict-free 16-byte loads (record stride 60 words). The copies complete
+// by a hardware wait (cp.async.wait_group), not a software spin, so no wait
+// can give up with a copy in flight, and the CTA drains every copy it issued
+// before it exits. Besides the splat, each (view, Gaussian) gets a
 // depth-sort key (view << 32 | bits(viewZ)) whose digit histograms are
 // accumulated here, and the digits of the tile ids its keys will carry are
 // counted from its tile rectangle for the key sort (count_tile_row). The tile
@@ -243,7 +247,8 @@ __device__ __forceinline__ uint32_t project_one(const Rec& rec, const float* em,
 
 // Persistent CTAs over chunks of kPreThreads records: while a chunk is
 // projected, the next chunk's records stream into the other shared-memory
-// stage (one TMA bulk copy each), so HBM reads overlap the arithmetic.
+// stage (asynchronous 16-byte copies, one commit group per chunk), so HBM
+// reads overlap the arithmetic.
 constexpr uint32_t kPreStages = 2;
 constexpr uint32_t kDepthPassesMax = 5;  // depth keys: 32 bits + log2(256 views)
 
@@ -257,7 +262,6 @@ struct PreSmem {
     uint32_t tdiff[257];
     uint32_t tall;
     uint32_t thist[kTileDigitsMax - 1][256];
-    uint64_t bar[kPreStages];
     uint32_t kept;                                        // depth keys of visible items in this CTA
 };
 
@@ -305,28 +309,30 @@ __global__ void __launch_bounds__(kPreThreads, 3) preprocess_kernel(PreprocessAr
     const uint32_t ndig = min(kTileDigitsMax, (a.tile_bits + 7) / 8);  // 0: no tile-digit counts
     if (tid == 0) S.kept = 0;
     uint32_t kept = 0;  // this thread's visible items (the depth sort drops the others)
-    if (tid == 0) {
-        for (uint32_t st = 0; st < kPreStages; ++st) mbar_init(&S.bar[st], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
     const uint32_t nchunks = (a.n + kPreThreads - 1) / kPreThreads;
     const uint32_t npass = min(kDepthPassesMax, (a.depth_key_bits + 7) / 8);
+    // chunk's records into stage: piece q (16 bytes) by thread q % 128, so a
+    // warp's copies are 512 consecutive bytes; a record is 15 whole pieces
     auto issue = [&](uint32_t chunk, uint32_t stage) {
         const uint32_t base = chunk * kPreThreads;
-        const uint32_t bytes = min(kPreThreads, a.n - base) * kRecordBytes;  // multiple of 16 (240 = 15 x 16)
-        mbar_arrive_expect_tx(&S.bar[stage], bytes);
-        bulk_copy_g2s(S.rec[stage], a.recs + size_t(base) * kRecordFloats, bytes, &S.bar[stage]);
+        const uint32_t pieces = min(kPreThreads, a.n - base) * (kRecordBytes / 16u);
+        const char* src = reinterpret_cast<const char*>(a.recs + size_t(base) * kRecordFloats);
+        char* dst = reinterpret_cast<char*>(S.rec[stage]);
+        for (uint32_t q = tid; q < pieces; q += kPreThreads) cp_async16(dst + 16u * q, src + 16u * q);
     };
-    if (tid == 0 && blockIdx.x < nchunks) issue(blockIdx.x, 0);
+    if (blockIdx.x < nchunks) issue(blockIdx.x, 0);
+    cp_async_commit();
 
     uint32_t it = 0;
     for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, ++it) {
-        const uint32_t stage = it & 1u, parity = (it >> 1) & 1u;
-        // the other stage was released by the barrier that ended the last iteration
-        if (tid == 0 && chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, stage ^ 1u);
-        bool staged = mbar_wait_bounded(&S.bar[stage], parity, &a.ctl->status);
-        if (!staged) mbar_wait_bounded(&S.bar[stage], parity, &a.ctl->status, 1u << 26);  // never leave a copy in flight
+        const uint32_t stage = it & 1u;
+        // the other stage was released by the barrier that ended the last
+        // iteration; a commit group per iteration (empty after the last
+        // chunk) keeps "all but the newest group" = this chunk
+        if (chunk + gridDim.x < nchunks) issue(chunk + gridDim.x, stage ^ 1u);
+        cp_async_commit();
+        cp_async_wait_all_but_newest();  // this thread's pieces of the chunk have landed
+        __syncthreads();                 // and every other thread's
 
         const uint32_t base = chunk * kPreThreads;
         const uint32_t cnt = min(kPreThreads, a.n - base);
@@ -336,7 +342,7 @@ __global__ void __launch_bounds__(kPreThreads, 3) preprocess_kernel(PreprocessAr
             Splat sp;
             uint4 rect = make_uint4(0u, 0u, 0u, 0u);
             uint32_t tiles = 0;
-            if (tid < cnt && staged) {
+            if (tid < cnt) {
                 const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
                 float emr[kEntityMatFloats];
 #pragma unroll
@@ -397,6 +403,7 @@ __global__ void __launch_bounds__(kPreThreads, 3) preprocess_kernel(PreprocessAr
         }
         __syncthreads();  // every thread is done with this stage before it is refilled
     }
+    cp_async_wait_all();  // nothing is left in flight (the last groups are empty)
     if (ndig) {
         __syncthreads();
         // digit 0: inclusive prefix of the difference array (two values per
@@ -530,15 +537,20 @@ void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, 
     frame_begin_kernel<<<1, 256, 0, s>>>(ctl, transforms, n_ent, views, n_views, ent_mats);
 }
 
+namespace {
+// The shared-memory opt-in (PreSmem is above 48 KB) and the resident CTAs per
+// SM, for the current device.
+int preprocess_setup() {
+    cudaFuncSetAttribute(preprocess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(PreSmem)));
+    int r = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, preprocess_kernel, kPreThreads, sizeof(PreSmem));
+    return r > 0 ? r : 1;
+}
+}  // namespace
+
 void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s) {
     if (a.n == 0 || a.n_views == 0) return;
-    static int per_sm = 0;  // resident CTAs per SM at this shared-memory size (same on every GB300)
-    if (per_sm == 0) {
-        cudaFuncSetAttribute(preprocess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(PreSmem)));
-        int r = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, preprocess_kernel, kPreThreads, sizeof(PreSmem));
-        per_sm = r > 0 ? r : 1;
-    }
+    const int per_sm = device_once(preprocess_setup);
     const uint32_t chunks = (a.n + kPreThreads - 1) / kPreThreads;
     const uint32_t blocks = std::min<uint32_t>(chunks, uint32_t((num_sms > 0 ? num_sms : 148) * per_sm));
     preprocess_kernel<<<blocks, kPreThreads, sizeof(PreSmem), s>>>(a);

@@ -20,6 +20,12 @@
 //    share it and race; order them on one stream.
 //  - Nothing has to start at zero: every call clears the descriptors and the
 //    control block's counters on the stream before the scan runs.
+//  - The address is looked up in the device's primary context (the one the
+//    runtime uses by default) and kept for the life of the process: calls
+//    from another driver context, or after cudaDeviceReset, are not
+//    supported.
+//  - A look-back wait that runs out leaves wrong offsets; the status output
+//    reports it (TPD_DEVSTAT_LOOKBACK_TIMEOUT).
 #include <cstdint>
 #include <mutex>
 
@@ -62,7 +68,8 @@ int scratch_for_current_device(unsigned char** out) {
 
 extern "C" {
 
-int tpd_scan_tiles_static(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total, void* stream) {
+int tpd_scan_tiles_static(const void* splats, uint32_t n, uint32_t* offsets, uint32_t* total, uint32_t* status,
+                          void* stream) {
     if (!total) return TPD_ERR_ARG;
     if (n > 0 && (!splats || !offsets)) return TPD_ERR_ARG;
     if (n > TPD_SCAN_STATIC_MAX_SPLATS) return TPD_ERR_CAPACITY;
@@ -75,8 +82,11 @@ int tpd_scan_tiles_static(const void* splats, uint32_t n, uint32_t* offsets, uin
     const size_t entries = size_t(n) / kStaticScanTile + 2;
     if (cudaMemsetAsync(desc, 0, entries * sizeof(uint64_t), s) != cudaSuccess) return TPD_ERR_DEVICE;
     launch_sort_begin(ctl, 0, s);
-    launch_scan_tiles(static_cast<const Splat*>(splats), n, offsets, desc, ctl, kStaticSpin, 0, s);
+    launch_scan_tiles(static_cast<const Splat*>(splats), n, offsets, desc, ctl, kStaticSpin,
+                      test_never_publish_standalone(), s);
     if (cudaMemcpyAsync(total, &ctl->total_keys, 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return TPD_ERR_DEVICE;
+    if (status && cudaMemcpyAsync(status, &ctl->status, 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return TPD_ERR_DEVICE;
     return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;
 }
 

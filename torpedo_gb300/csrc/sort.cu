@@ -53,7 +53,7 @@ constexpr int kPassDropCulled = 1; // as plain; keys whose low 32 bits are 0xFFF
 constexpr int kPassCompacted = 2;  // K = ctl->depth_count; a uniform digit makes the pass a copy
 
 constexpr uint32_t kHistThreads = 256;
-constexpr uint32_t kHistChunk = 2048;  // keys per TMA chunk (16 KB)
+constexpr uint32_t kHistChunk = 2048;  // keys per grid-stride chunk of the histogram kernel
 
 // Reorder buffers hold one pad slot per 16 keys: digit runs of about 16 keys
 // (8-bit digits over a 4096-key partition) put the runs of consecutive digits
@@ -480,25 +480,28 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 // (128 registers, no spills; the default) or 3 (80 registers); the 512-thread,
 // 8-key variant for 2 (32 warps per SM); the 8- and 4-key 256-thread variants
 // (shorter partitions, for small sorts) for 4 and 5.
+// Shared-memory opt-in of every pass kind of a variant and its resident CTAs
+// per SM, once per device.
+template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+int onesweep_setup() {
+    const size_t smem = sizeof(OnesweepSmem<kItems, kThreads, KeyT>);
+    cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain, KeyT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if constexpr (sizeof(KeyT) == 8) {
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled, KeyT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted, KeyT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    }
+    int r = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain, KeyT>,
+                                                  kThreads, smem);
+    return r > 0 ? r : 1;
+}
+
 template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
 int onesweep_occupancy() {
-    static int b = 0;
-    if (b == 0) {
-        const size_t smem = sizeof(OnesweepSmem<kItems, kThreads, KeyT>);
-        cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain, KeyT>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if constexpr (sizeof(KeyT) == 8) {
-            cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled, KeyT>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-            cudaFuncSetAttribute(onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted, KeyT>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        }
-        int r = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, onesweep_kernel<kItems, kThreads, kMinBlocks, kPassPlain, KeyT>,
-                                                      kThreads, smem);
-        b = r > 0 ? r : 1;
-    }
-    return b;
+    return device_once(onesweep_setup<kItems, kThreads, kMinBlocks, KeyT>);
 }
 
 template <int kItems, int kThreads, int kMinBlocks, typename KeyT>

@@ -8,6 +8,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/tpdsplat.h"
+
 namespace tpd {
 
 constexpr uint32_t kBlockX = 16;          // tile width in pixels
@@ -19,11 +21,14 @@ constexpr uint32_t kRecordBytes = 240;
 // Status bits written by kernels to the device status word (never traps).
 constexpr uint32_t kStatusKeyOverflow = 1u << 0;     // more keys than key capacity
 constexpr uint32_t kStatusLookbackTimeout = 1u << 1; // a decoupled look-back spin ran out
-constexpr uint32_t kStatusMbarTimeout = 1u << 2;     // a TMA mbarrier wait ran out
+constexpr uint32_t kStatusMbarTimeout = 1u << 2;     // reserved: no kernel waits on an mbarrier
 constexpr uint32_t kStatusBadInput = 1u << 3;        // an input outside the documented range
 constexpr uint32_t kStatusBadIndex = 1u << 4;        // checked builds: an index failed its bounds check
 // Statuses after which the rest of the frame is skipped (its lists are unusable).
 constexpr uint32_t kStatusFatal = kStatusLookbackTimeout | kStatusMbarTimeout;
+static_assert(kStatusKeyOverflow == TPD_DEVSTAT_KEY_OVERFLOW && kStatusLookbackTimeout == TPD_DEVSTAT_LOOKBACK_TIMEOUT &&
+                  kStatusBadInput == TPD_DEVSTAT_BAD_INPUT && kStatusBadIndex == TPD_DEVSTAT_BAD_INDEX,
+              "device status bits as the C ABI documents them");
 
 // Splat record: color[3], tiles, texel = (px, py, viewZ, radius), copac = (conic.xyz, opacity).
 struct __align__(16) Splat {
@@ -55,50 +60,18 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+// 16-byte asynchronous copy global -> shared (cp.async, L2 only), grouped
+// by cp_async_commit and completed by the hardware waits below: a thread
+// waits for its own copies; a barrier afterwards publishes them to the CTA.
+// Both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
-
-__device__ __forceinline__ void fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// One-dimensional bulk copy global -> shared, completing on an mbarrier.
-// dst, src 16-byte aligned; bytes a multiple of 16.
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(phase)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait on an mbarrier phase. Returns false (and sets the status bit)
-// when the limit runs out; the caller then skips the staged data.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, uint32_t* status,
-                                                  uint32_t limit = (1u << 20)) {
-    for (uint32_t i = 0; i < limit; ++i)
-        if (mbar_try_wait(bar, phase)) return true;
-    atomicOr(status, kStatusMbarTimeout);
-    return false;
-}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Every committed group of this thread but the newest has completed.
+__device__ __forceinline__ void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+// Every committed group of this thread has completed.
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Relaxed, device-scope 64-bit load / store: single-copy atomic, used for
 // self-contained look-back descriptors (flag + tag + value in one word).
@@ -133,17 +106,20 @@ __device__ __forceinline__ uint32_t desc_flag(uint64_t d, uint32_t tag) {
 __device__ __forceinline__ int trunc_to_int(float v) { return __float2int_rz(v); }
 
 // getBoundingRect (splat/volume.slang:12-17). Same float operations as the shader:
-// ((p - r) / 16) and ((p + r) + 15) / 16, truncated toward zero, clamped to the grid.
+// ((p - r) / 16) and (p + r + 16 - 1) / 16, the latter two rounded additions
+// ((p + r) + 16) then a rounded subtraction of 1, left to right as the shader
+// writes p + r + BLOCK_X - 1 (which can differ from (p + r) + 15 when p + r + 16
+// crosses a power of two), truncated toward zero and clamped to the grid.
 // Dividing by 16 is multiplying by 2^-4: both round the same exact quotient,
 // so the product gives the division's result bit for bit.
-static_assert(kBlockX == 16, "the tile rect divides by 16 as a multiply by 2^-4");
+static_assert(kBlockX == 16 && kBlockY == 16, "the tile rect divides by 16 as a multiply by 2^-4");
 __device__ __forceinline__ void bounding_rect(float px, float py, float radius, uint32_t gx, uint32_t gy,
                                               uint32_t& x0, uint32_t& y0, uint32_t& x1, uint32_t& y1) {
-    const float inv = 0.0625f, b1 = float(kBlockX - 1);
+    const float inv = 0.0625f, bx = float(kBlockX);
     const int a = trunc_to_int(__fmul_rn(__fsub_rn(px, radius), inv));
     const int b = trunc_to_int(__fmul_rn(__fsub_rn(py, radius), inv));
-    const int c = trunc_to_int(__fmul_rn(__fadd_rn(__fadd_rn(px, radius), b1), inv));
-    const int d = trunc_to_int(__fmul_rn(__fadd_rn(__fadd_rn(py, radius), b1), inv));
+    const int c = trunc_to_int(__fmul_rn(__fsub_rn(__fadd_rn(__fadd_rn(px, radius), bx), 1.0f), inv));
+    const int d = trunc_to_int(__fmul_rn(__fsub_rn(__fadd_rn(__fadd_rn(py, radius), bx), 1.0f), inv));
     x0 = min(gx, uint32_t(max(0, a)));
     y0 = min(gy, uint32_t(max(0, b)));
     x1 = min(gx, uint32_t(max(0, c)));

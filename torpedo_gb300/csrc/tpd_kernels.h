@@ -61,6 +61,15 @@ struct PreprocessArgs {
 
 constexpr uint32_t kMaxViews = 256;
 
+// Kernel set-up that must happen once per device (a shared-memory opt-in, an
+// occupancy query): calls init() the first time it is asked for on the
+// current device and returns that result on every later call there.
+// Thread-safe; keyed by (device, init).
+int device_once(int (*init)());
+
+// The test hook of the standalone scans (tpd_test_set_never_publish).
+uint32_t test_never_publish_standalone();
+
 // Clears tickets, histograms and status of ctl and advances its tag; computes
 // entity matrices for n_views x n_ent (transforms nullptr -> identity).
 void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, const ViewConst* views,

@@ -353,7 +353,21 @@ def sort_pairs(keys, vals, key_bits: int):
     stream = torch.cuda.current_stream(keys.device).cuda_stream
     _check(lib.tpd_sort_pairs(keys.data_ptr(), vals.data_ptr(), ka.data_ptr(), va.data_ptr(), n, key_bits,
                               ws.data_ptr(), ws.numel(), stream, C.byref(alt)))
+    _check_workspace_status(ws, n)
     return (ka, va) if alt.value else (keys, vals)
+
+
+def _check_workspace_status(ws, n: int) -> None:
+    """Raises TpdError when the device status word a stage call left in its
+    workspace is not 0 (waits for the stream)."""
+    import torch
+
+    if n == 0:
+        return
+    st = int(ws[L.WORKSPACE_STATUS_OFFSET:L.WORKSPACE_STATUS_OFFSET + 4].view(torch.int32).item())
+    if st:
+        raise L.TpdError(L.TPD_ERR_TIMEOUT if st & L.DEVSTAT_LOOKBACK_TIMEOUT else L.TPD_ERR_DEVICE,
+                         f"device status 0x{st & 0xFFFFFFFF:x}: the result is invalid")
 
 
 def scan_tiles(splats_u32):
@@ -368,4 +382,5 @@ def scan_tiles(splats_u32):
     stream = torch.cuda.current_stream(splats_u32.device).cuda_stream
     _check(lib.tpd_scan_tiles(splats_u32.data_ptr(), n, offs.data_ptr(), tot.data_ptr(), ws.data_ptr(), ws.numel(),
                               stream))
+    _check_workspace_status(ws, n)
     return offs, tot
