@@ -18,25 +18,24 @@
 //  - (int) of a float truncates toward zero and saturates (NaN -> 0).
 //  - min / max of floats return the non-NaN operand (fmin / fmax); of an
 //    unsigned and a signed integer, the signed one is converted first.
-//  - a workgroup's invocations run as OS threads that meet at
+//  - a workgroup's invocations are fibers of one host thread that meet at
 //    GroupMemoryBarrierWithGroupSync; an invocation that returns leaves the
-//    barriers of its workgroup. Workgroups of a dispatch run one after
-//    another, in the order of their index (so a decoupled look-back always
-//    finds its predecessors done).
+//    barriers of its workgroup. Workgroups start in the order of their index
+//    and run concurrently on the host's cores (see dispatch below).
 //  - buffers check every index: an access past the end reads 0 and drops the
 //    write (robust buffer access) and is counted in oob_accesses().
 #pragma once
 
+#include <ucontext.h>
+
+#include <algorithm>
 #include <array>
 #include <atomic>
-#include <barrier>
 #include <cmath>
-#include <condition_variable>
 #include <cstdint>
 #include <cstring>
 #include <functional>
 #include <limits>
-#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -280,75 +279,91 @@ inline void InterlockedCompareExchange(uint64_t& dst, uint64_t cmp, uint64_t v, 
 }
 
 // ---------------------------------------------------------------- workgroups
+//
+// A workgroup runs on one host thread: its invocations are fibers (ucontext)
+// that the thread switches between, and GroupMemoryBarrierWithGroupSync
+// switches out of the calling invocation. The thread resumes every
+// unfinished invocation in turn; since invocations give up control only at
+// barriers (or by returning), one pass over them brings every live
+// invocation to the same barrier, which is a barrier's meaning. Groupshared
+// variables are thread_local, so each workgroup has its own.
+//
+// The workgroups of a dispatch start in the order of their index and run
+// concurrently on the host's cores; a workgroup, once started, runs to
+// completion, so a decoupled look-back (whose partitions are numbered by an
+// atomic counter at the start of each workgroup) always waits on running
+// workgroups only.
 
-// The barrier of one workgroup; invocations that have returned no longer
-// take part.
-struct Workgroup {
-    std::mutex m;
-    std::condition_variable cv;
-    uint32_t active = 0, arrived = 0;
-    uint64_t generation = 0;
-
-    void reset(uint32_t n) {
-        std::lock_guard<std::mutex> lock(m);
-        active = n;
-        arrived = 0;
-    }
-    void sync() {
-        std::unique_lock<std::mutex> lock(m);
-        const uint64_t g = generation;
-        if (++arrived == active) {
-            arrived = 0;
-            ++generation;
-            cv.notify_all();
-            return;
-        }
-        cv.wait(lock, [&] { return generation != g; });
-    }
-    void leave() {
-        std::lock_guard<std::mutex> lock(m);
-        --active;
-        if (active > 0 && arrived == active) {
-            arrived = 0;
-            ++generation;
-            cv.notify_all();
-        }
-    }
+struct FiberGroup {
+    ucontext_t sched{};
+    std::vector<ucontext_t> ctx;
+    std::vector<std::vector<char>> stacks;
+    std::vector<uint8_t> done;
+    uint32_t current = 0;
+    uint3 gid{0, 0, 0}, wg{1, 1, 1};
+    const std::function<void(uint3, uint3, uint3)>* entry = nullptr;
 };
 
-inline Workgroup*& current_workgroup() {
-    thread_local Workgroup* wg = nullptr;
-    return wg;
+inline FiberGroup*& current_group() {
+    thread_local FiberGroup* g = nullptr;
+    return g;
 }
 
-inline void GroupMemoryBarrierWithGroupSync() { current_workgroup()->sync(); }
+inline void GroupMemoryBarrierWithGroupSync() {
+    FiberGroup* g = current_group();
+    swapcontext(&g->ctx[g->current], &g->sched);
+}
+
+inline void fiber_main() {
+    FiberGroup* g = current_group();
+    const uint32_t t = g->current;
+    const uint3 gtid(t % g->wg.x, (t / g->wg.x) % g->wg.y, t / (g->wg.x * g->wg.y));
+    const uint3 dtid(g->gid.x * g->wg.x + gtid.x, g->gid.y * g->wg.y + gtid.y, g->gid.z * g->wg.z + gtid.z);
+    (*g->entry)(gtid, g->gid, dtid);
+    g->done[t] = 1;  // returning resumes the scheduler (uc_link)
+}
 
 // Runs entry(group thread id, group id, dispatch thread id) for every
 // invocation of groups.x x groups.y x groups.z workgroups of size wg.
 inline void dispatch(uint3 groups, uint3 wg, const std::function<void(uint3, uint3, uint3)>& entry) {
+    constexpr size_t kStack = 64 * 1024;
     const uint64_t ngroups = uint64_t(groups.x) * groups.y * groups.z;
     const uint32_t nthreads = wg.x * wg.y * wg.z;
     if (ngroups == 0 || nthreads == 0) return;
-    Workgroup group;
-    std::barrier<> between(nthreads);
-    std::vector<std::thread> pool;
-    pool.reserve(nthreads);
-    for (uint32_t t = 0; t < nthreads; ++t) {
-        pool.emplace_back([&, t] {
-            current_workgroup() = &group;
-            const uint3 gtid(t % wg.x, (t / wg.x) % wg.y, t / (wg.x * wg.y));
-            for (uint64_t g = 0; g < ngroups; ++g) {
-                if (t == 0) group.reset(nthreads);
-                between.arrive_and_wait();  // the group's barrier is reset before anyone uses it
-                const uint3 gid(uint(g % groups.x), uint((g / groups.x) % groups.y),
-                                uint(g / (uint64_t(groups.x) * groups.y)));
-                const uint3 dtid(gid.x * wg.x + gtid.x, gid.y * wg.y + gtid.y, gid.z * wg.z + gtid.z);
-                entry(gtid, gid, dtid);
-                group.leave();
-                between.arrive_and_wait();  // every invocation of this group has returned
+    std::atomic<uint64_t> next{0};
+    const uint32_t workers = uint32_t(std::min<uint64_t>(ngroups, std::max(1u, std::thread::hardware_concurrency())));
+    auto worker = [&] {
+        FiberGroup fg;
+        fg.ctx.resize(nthreads);
+        fg.stacks.assign(nthreads, std::vector<char>(kStack));
+        fg.done.assign(nthreads, 0);
+        fg.wg = wg;
+        fg.entry = &entry;
+        current_group() = &fg;
+        for (uint64_t g = next.fetch_add(1); g < ngroups; g = next.fetch_add(1)) {
+            fg.gid = uint3(uint(g % groups.x), uint((g / groups.x) % groups.y), uint(g / (uint64_t(groups.x) * groups.y)));
+            for (uint32_t t = 0; t < nthreads; ++t) {
+                getcontext(&fg.ctx[t]);
+                fg.ctx[t].uc_stack.ss_sp = fg.stacks[t].data();
+                fg.ctx[t].uc_stack.ss_size = kStack;
+                fg.ctx[t].uc_link = &fg.sched;
+                makecontext(&fg.ctx[t], fiber_main, 0);
+                fg.done[t] = 0;
             }
-        });
-    }
+            for (uint32_t live = nthreads; live > 0;) {
+                for (uint32_t t = 0; t < nthreads; ++t) {
+                    if (fg.done[t]) continue;
+                    fg.current = t;
+                    swapcontext(&fg.sched, &fg.ctx[t]);
+                    if (fg.done[t]) --live;
+                }
+            }
+        }
+        current_group() = nullptr;
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t w = 1; w < workers; ++w) pool.emplace_back(worker);
+    worker();
     for (auto& th : pool) th.join();
 }
 

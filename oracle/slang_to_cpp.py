@@ -12,8 +12,9 @@ the workgroup execution model):
 
   import splat; / module / implementing  the module's text, translated, included once per shader
   __include "f"                          the translated text of f, inline
-  public, groupshared, uniform, attributes ([[...]], [shader], [numthreads], [SpecializationConstant])
+  public, uniform, attributes ([[...]], [shader], [numthreads], [SpecializationConstant])
                                          dropped ([numthreads] is kept as the shader's workgroup size)
+  groupshared                            thread_local (a workgroup runs on one host thread)
   let x = e / var x = e                  const auto x = e / auto x = e
   out T x / inout T x (parameters)       T& x
   v.xy / v.xyz (swizzles)                v.xy() / v.xyz()
@@ -44,7 +45,8 @@ def _float_literals(text: str) -> str:
 
 def _translate_code(code: str) -> str:
     code = re.sub(r"\bConstantBuffer<float4\[4\]>\.Handle\b", "TransformHandle", code)
-    code = re.sub(r"\b(public|groupshared|uniform)\s+", "", code)
+    code = re.sub(r"\b(public|uniform)\s+", "", code)
+    code = re.sub(r"\bgroupshared\s+", "thread_local ", code)
     code = re.sub(r"\blet\s+", "const auto ", code)
     code = re.sub(r"\bvar\s+", "auto ", code)
     code = re.sub(r"([(,])([ \t]*)(?:out|inout)[ \t]+(\w+)[ \t]+(\w+)", r"\1\2\3& \4", code)

@@ -8,7 +8,14 @@ with oracle/build_ref.py and records
                        getHigherMSB table, and GaussianPoint::fromModel records
                        of the PLY files below
   ply_*.ply            small seeded 3DGS PLY files (binary and ASCII)
-The tests compare libtpdsplat's host code against these, bit for bit.
+  reference_shaders.npz  (`make_golden.py shaders`) frames of the scenes in
+                       shader_scenes.py run through the reference's own
+                       compute shaders (their Slang source, translated and run
+                       on the CPU by oracle/ref_shaders.cpp): K, pass count and
+                       SHA-256 digests of splats, offsets, sorted keys and
+                       values, ranges and image; the arrays of small scenes
+The tests compare libtpdsplat's host code, the oracle and the CUDA pipeline
+against these.
 """
 from __future__ import annotations
 
@@ -120,5 +127,46 @@ def main():
     print("wrote", HERE / "reference_host.npz", {k: v.shape for k, v in out.items()})
 
 
+def shaders():
+    import time
+
+    from oracle import reference
+    from tests.golden import shader_scenes as SS
+
+    out = {}
+    names = []
+    for name, sc in SS.build_scenes().items():
+        t0 = time.perf_counter()
+        r = reference.frame(sc["records"], sc["view"], sc["projview"], sc["focal"], sc["width"], sc["height"],
+                            sc["sh_degree"], sc["ent_idx"], sc["transforms"])
+        assert r["oob"] == 0, f"{name}: {r['oob']} out-of-range buffer accesses"
+        n = sc["records"].shape[0]
+        out[f"{name}/meta"] = np.array([sc["width"], sc["height"], sc["sh_degree"], r["K"], r["passes"], n], np.int64)
+        for k in ("view", "proj", "projview", "focal"):
+            out[f"{name}/{k}"] = sc[k]
+        if sc["gen"] is not None:
+            out[f"{name}/gen"] = np.array(sc["gen"], np.float64)
+        else:
+            out[f"{name}/records"] = sc["records"]
+        if sc["ent_idx"] is not None:
+            out[f"{name}/ent_idx"] = sc["ent_idx"]
+            out[f"{name}/transforms"] = sc["transforms"]
+        for k in ("splats", "offsets", "keys", "vals", "ranges", "image"):
+            out[f"{name}/sha_{k}"] = np.array(SS.digest(r[k]))
+        if r["K"] <= SS.SMALL_KEYS:
+            for k in ("splats", "keys", "vals", "ranges"):
+                out[f"{name}/{k}"] = r[k]
+        if sc["width"] * sc["height"] <= SS.SMALL_PIXELS:
+            out[f"{name}/image"] = r["image"][..., :3]
+        names.append(name)
+        print(f"{name}: K={r['K']} passes={r['passes']} ({time.perf_counter() - t0:.1f} s)", flush=True)
+    out["scenes"] = np.array(names)
+    np.savez_compressed(SS.FIXTURE, **out)
+    print("wrote", SS.FIXTURE, SS.FIXTURE.stat().st_size, "bytes")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "shaders":
+        shaders()
+    else:
+        main()

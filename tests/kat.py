@@ -146,3 +146,36 @@ def wide_row():
                            float(rng.uniform(0.3, 0.9)), tuple(float(v) for v in rng.uniform(0.02, 0.1, 3)),
                            sh=rgb2sh(*(float(c) for c in rng.uniform(0, 1, 3)))))
     return np.stack(recs), cam
+
+
+def _f32_bits(bits: int) -> float:
+    return float(np.array([bits], np.uint32).view(np.float32)[0])
+
+
+def _edge_scene(cam, axis: int, coord_bits: int):
+    """One Gaussian placed (by a search over float positions) so that its
+    centre plus radius is exactly 1009 - 2^-14 pixels along `axis`, plus 20
+    ordinary ones. The shader's rect bound p + r + BLOCK - 1 adds 16 first:
+    1024.99994 rounds (ties to even) to 1025, so after the - 1 the bound is
+    1024 / 16 = 64, one tile more than (p + r) + 15 = 1023.99994 would give."""
+    pos = [0.0, 0.0, 0.0]
+    pos[axis] = _f32_bits(coord_bits)
+    recs = [record(tuple(pos), 0.8, (0.004, 0.004, 0.004), sh=rgb2sh(0.9, 0.2, 0.4))]
+    rng = np.random.default_rng(15 + axis)
+    for _ in range(20):
+        p = [0.0, 0.0, float(rng.uniform(-1, 1))]
+        p[axis] = float(rng.uniform(-3, 3))
+        recs.append(record(tuple(p), float(rng.uniform(0.3, 0.9)), tuple(float(v) for v in rng.uniform(0.005, 0.05, 3)),
+                           sh=rgb2sh(*(float(c) for c in rng.uniform(0, 1, 3)))))
+    return np.stack(recs), cam
+
+
+def rect_edge_x():
+    """A 2048x48 view with a Gaussian whose right tile bound comes from the
+    rounding of p + r + 16 - 1 (see _edge_scene): 2 tiles, not 1."""
+    return _edge_scene(camera(2048, 48), 0, 0xC006B72F)
+
+
+def rect_edge_y():
+    """The same along y, on a 48x2048 view: 2 tiles, not 1."""
+    return _edge_scene(camera(48, 2048), 1, 0xBD612AD6)
