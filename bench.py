@@ -29,7 +29,9 @@ radix sort -> tile ranges -> blend, with the Gaussians resident in device memory
          forward + backward per step, with the key count and the device
          memory the engine holds
   autotune  the launch setting picked for the workload (torpedo_gb300.autotune)
-         and the per-frame time of each candidate
+         and the per-frame time of each candidate; train_ms_per_step the
+         training-step candidates (blend batch depths, persistent tile
+         scheduler) tuned on cfg2 and on cfg3, whose picks those runs use
 
 --impl reference times that CPU transcription alone (rank 0; other ranks exit).
 Launched with torchrun for N > 1: every rank renders the workload independently
@@ -319,6 +321,39 @@ def train_rate(cfg_name, stream, local, steps, warmup, settings, stage_steps=0):
     return ms, st, len(cams), pixels, stages, {"device_bytes_held": int(held)}
 
 
+def train_tune(cfg_name, stream, local, base, frames=4, warmup=2):
+    """The training-step autotuner (torpedo_gb300.autotune.TRAIN_AXES: the
+    blend's batch depths and its persistent form) on a config's forward +
+    backward step; returns (settings, {candidate: ms per step})."""
+    import torch
+
+    import torpedo_gb300 as T
+    from torpedo_gb300 import autotune, configs
+
+    dev = torch.device("cuda", local)
+    cfg = configs.CONFIGS[cfg_name]
+    sc = configs.scene(cfg)
+    cams = configs.cameras(cfg)
+    params = _params(sc, dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(cfg.name[3:]))
+    dimg = torch.randn(sum(c.width * c.height for c in cams) * 3, generator=gen, device=dev)
+    grads = [torch.empty_like(p) for p in params]
+
+    def make(settings):
+        e = T.GaussianEngine(device=local, stream=stream.cuda_stream, **settings)
+        e.compile_params(*params)
+        if len(cams) == 1:
+            e.set_camera(cams[0])
+        else:
+            e.set_views(cams)
+        e.raster_frame()
+        return e
+
+    return autotune.tune(make, lambda e, k: e.step_async(dimg, grads, k), stream, frames=frames, warmup=warmup,
+                         axes=autotune.TRAIN_AXES, base=base)
+
+
 def plain_views_rate(cfg_name, local, passes, settings):
     """The plain pipeline on the same views: per view set_camera, raster_frame
     and backward, each call returning when its work is done (one engine per
@@ -525,15 +560,18 @@ def run_ours(args):
                      "note": "20 FP32 operations per evaluated pair; peak = SMs x 128 FP32 lanes x 2 x max SM clock"}
 
     fwd_bwd = batched = large = None
+    tuned_train = {}
     if not args.no_train:
-        ms2, st2, _, _, _, _ = train_rate("cfg2", stream, local, 50, 3, settings)
+        settings2, tuned_train["cfg2"] = train_tune("cfg2", stream, local, settings, frames=20, warmup=3)
+        ms2, st2, _, _, _, _ = train_rate("cfg2", stream, local, 50, 3, settings2)
         fwd_bwd = {"config": "cfg2: 200,000 Gaussians (means N(0,1)^3), one 800x800 view, dL/dimage ~ N(0,1)",
                    "value": round(1000.0 / ms2, 3), "unit": "it/s", "ms_per_step": round(ms2, 4),
-                   "keys": int(st2["keys"]),
+                   "keys": int(st2["keys"]), "settings": settings2,
                    "step": "forward frame + backward to means, log-scales, quaternions, opacity logits, SH; "
                            "one captured CUDA graph per step"}
-        ms3, st3, views3, pixels3, stages3, _ = train_rate("cfg3", stream, local, 5, 2, settings, stage_steps=2)
-        plain = plain_views_rate("cfg3", local, 3, settings)
+        settings3, tuned_train["cfg3"] = train_tune("cfg3", stream, local, settings)
+        ms3, st3, views3, pixels3, stages3, _ = train_rate("cfg3", stream, local, 5, 2, settings3, stage_steps=2)
+        plain = plain_views_rate("cfg3", local, 3, settings3)
         batched = {"config": "cfg3: 500,000 Gaussians (means N(0,1)^3), 64 views on a sphere of radius 5, sizes "
                              "from {640x480, 1280x720, 1920x1080} (seed 3), dL/dimage ~ N(0,1)",
                    "views_per_s": round(views3 * 1000.0 / ms3, 2), "ms_per_step": round(ms3, 3),
@@ -541,10 +579,10 @@ def run_ours(args):
                    "plain_views_per_s": round(plain, 2), "batched_over_plain": round(views3 * 1000.0 / ms3 / plain, 3),
                    "plain": "one view per call: set_camera, raster_frame, backward, each waiting for its work; "
                             "fastest of 3 passes over the 64 views",
-                   "stages_ms": stages3,
+                   "stages_ms": stages3, "settings": settings3,
                    "stages_note": "per step, from 2 eager steps with CUDA events between stages (no graph)"}
         if not args.no_large:
-            ms4, st4, views4, pixels4, _, ex4 = train_rate("cfg4", stream, local, 3, 1, settings)
+            ms4, st4, views4, pixels4, _, ex4 = train_rate("cfg4", stream, local, 3, 1, settings3)
             large = {"config": "cfg4: 6,000,000 Gaussians (means U[-10,10]^3), 8 views of 3840x2160, "
                                "dL/dimage ~ N(0,1)",
                      "views_per_s": round(views4 * 1000.0 / ms4, 2), "ms_per_step": round(ms4, 3),
@@ -581,7 +619,7 @@ def run_ours(args):
         "stages_ms": {k: round(v, 4) for k, v in stage_avg.items()},
         "gpu_launches": launches_per_frame * args.steps,
         "clocks": clk,
-        "autotune": {"settings": settings, "ms_per_frame": tuned},
+        "autotune": {"settings": settings, "ms_per_frame": tuned, "train_ms_per_step": tuned_train},
         "fwd_bwd": fwd_bwd,
         "batched": batched,
         "large": large,

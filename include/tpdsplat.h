@@ -78,7 +78,11 @@ typedef struct tpd_settings {
     uint32_t sort_threads;         /* CTA size of the key sort's 4096-key radix passes: 512 x 8 keys (0 = default) or 256 x 16 */
     uint32_t depth_sort_threads;   /* CTA size of the depth sort's radix passes: 256 (0 = default) or 512 (8 keys each,
                                       whatever depth_sort_items says) */
-    uint32_t reserved[2];
+    uint32_t blend_round;          /* list entries the blend stages per round: 128 (0 = default), 64 or 256 */
+    uint32_t blend_backward_round; /* list entries the blend adjoint stages per round: 64 (0 = default), 32 or 128 */
+    uint32_t blend_persistent;     /* 1: the blend and its adjoint run persistent CTAs taking (view, tile) items from a
+                                      queue (the adjoint's longest lists first); 0 (default): one CTA per tile */
+    uint32_t reserved[3];
 } tpd_settings;
 
 /* Stages of a frame (and of a training step), for tpd_stage_times. */

@@ -73,8 +73,11 @@ def build(force: bool = False) -> Path:
             f"-I{REF / 'volumetric/src'}"]
     # the shaders: IEEE single precision, no contraction, threads for workgroups
     shader = ["-std=c++23", "-ffp-contract=off", "-fno-strict-aliasing", "-pthread", f"-I{HERE}", f"-I{OUT / 'gen'}"]
-    units = [(HERE / "ref_glue.cpp", host), (gen, host), (REF / "rendering/src/Camera.cpp", host),
-             (REF / "extension/src/PerspectiveCamera.cpp", host), (REF / "volumetric/src/GaussianGeometry.cpp", host),
+    # GaussianPoint::random seeds itself from std::random_device: the forced
+    # header makes that seed settable (see seeded_random_device.h)
+    seeded = [*host, f"-I{HERE}", "-include", str(HERE / "seeded_random_device.h")]
+    units = [(HERE / "ref_glue.cpp", [*host, f"-I{HERE}"]), (gen, host), (REF / "rendering/src/Camera.cpp", host),
+             (REF / "extension/src/PerspectiveCamera.cpp", host), (REF / "volumetric/src/GaussianGeometry.cpp", seeded),
              (REF / "volumetric/src/miniply.cpp", host), (HERE / "ref_shaders.cpp", shader)]
     objs = [OUT / f"{src.stem}.o" for src, _ in units]
     with ThreadPoolExecutor(max_workers=len(units)) as ex:

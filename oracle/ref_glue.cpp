@@ -13,10 +13,23 @@
 #include <torpedo/extension/PerspectiveCamera.h>
 #include <torpedo/volumetric/GaussianGeometry.h>
 
+#include "seeded_random_device.h"
+
 #include <cstdint>
 #include <cstring>
 
 uint32_t ref_higher_msb_impl(uint32_t n);  // generated from GaussianEngine.h
+
+namespace {
+unsigned int g_random_seed = 0;
+int g_arg_probe = 0;
+int arg_probe_next() { return g_arg_probe++; }
+int arg_probe_first(int a, int) { return a; }
+}  // namespace
+
+// The seed GaussianPoint::random draws from std::random_device (see
+// seeded_random_device.h).
+unsigned int std::tpd_seeded_random_device::operator()() const { return g_random_seed; }
 
 extern "C" {
 
@@ -52,6 +65,24 @@ uint32_t ref_from_model(const char* path, float* records, uint32_t cap) {
     const uint32_t n = static_cast<uint32_t>(pts.size());
     if (records) std::memcpy(records, pts.data(), sizeof(tpd::GaussianPoint) * std::min(n, cap));
     return n;
+}
+
+// GaussianPoint::random (GaussianGeometry.cpp:8-32) with its std::mt19937
+// seeded by `seed`: n records.
+void ref_random_points(uint32_t seed, uint32_t n, float radius, const float center[3], float min_scale,
+                       float max_scale, float min_opacity, float max_opacity, float* records) {
+    g_random_seed = seed;
+    const auto pts = tpd::GaussianPoint::random(n, radius, {center[0], center[1], center[2]}, min_scale, max_scale,
+                                                min_opacity, max_opacity);
+    std::memcpy(records, pts.data(), sizeof(tpd::GaussianPoint) * n);
+}
+
+// 1 when this build evaluates function arguments right to left (g++ does for
+// rgb2sh(dist_sh(rng), dist_sh(rng), dist_sh(rng)), GaussianGeometry.cpp:29;
+// clang, the reference's compiler, left to right).
+int ref_args_right_to_left() {
+    g_arg_probe = 0;
+    return arg_probe_first(arg_probe_next(), arg_probe_next()) == 1 ? 1 : 0;
 }
 
 }  // extern "C"

@@ -43,6 +43,9 @@ def ref_lib():
     lib.ref_gaussian_point_size.restype = C.c_uint32
     lib.ref_from_model.argtypes = [C.c_char_p, F, C.c_uint32]
     lib.ref_from_model.restype = C.c_uint32
+    lib.ref_random_points.argtypes = [C.c_uint32, C.c_uint32, C.c_float, F, C.c_float, C.c_float, C.c_float,
+                                      C.c_float, F]
+    lib.ref_args_right_to_left.restype = C.c_int
     return lib
 
 
@@ -122,6 +125,21 @@ def main():
         rec = np.zeros((cnt, 60), np.float32)
         lib.ref_from_model(str(path).encode(), fp(rec), cnt)
         out[f"{name}_records"] = rec
+
+    # GaussianPoint::random with its generator seeded: (seed, n, radius, center xyz, scale and opacity bounds)
+    rp_args = np.array([[1, 64, 2.5, 0.1, -0.2, 0.3, 0.01, 0.1, 0.2, 0.9],
+                        [7, 40, 10.0, 0.0, 0.0, 0.0, 0.005, 0.2, 0.1, 1.0]], np.float32)
+    rp = []
+    for a in rp_args:
+        rec = np.zeros((int(a[1]), 60), np.float32)
+        ctr = np.ascontiguousarray(a[3:6])
+        lib.ref_random_points(int(a[0]), int(a[1]), float(a[2]), fp(ctr), float(a[6]), float(a[7]), float(a[8]),
+                              float(a[9]), fp(rec))
+        rp.append(rec)
+    out["random_args"] = rp_args
+    out["random_records"] = np.stack(rp[:1])[0]
+    out["random_records_b"] = rp[1]
+    out["random_args_right_to_left"] = np.array(lib.ref_args_right_to_left(), np.int32)
 
     np.savez_compressed(HERE / "reference_host.npz", **out)
     print("wrote", HERE / "reference_host.npz", {k: v.shape for k, v in out.items()})

@@ -94,3 +94,21 @@ def test_ply_loader_errors(tmp_path):
         T.load_ply(bad)
     with pytest.raises(T.TpdError):
         T.load_ply(tmp_path / "missing.ply")
+
+
+@pytest.mark.parametrize("key,row", [("random_records", 0), ("random_records_b", 1)])
+def test_random_points_match_the_reference_generator(gold, key, row):
+    """GaussianPoint::random (GaussianGeometry.cpp:8-32) with its mt19937
+    seeded: positions, opacities, quaternions, scales and SH bit for bit. The
+    reference fills the DC colour with rgb2sh(dist_sh(rng), dist_sh(rng),
+    dist_sh(rng)), whose argument order C++ leaves to the compiler: clang, the
+    reference's own (README.md:116), evaluates left to right, as tpd_random_points
+    does; the g++ build that recorded the fixture evaluates right to left
+    (random_args_right_to_left), which swaps the red and blue draws."""
+    a = gold["random_args"][row]
+    ref = gold[key].copy()
+    got = T.random_points(int(a[0]), int(a[1]), float(a[2]), tuple(float(x) for x in a[3:6]), float(a[6]), float(a[7]),
+                          float(a[8]), float(a[9]))
+    if int(gold["random_args_right_to_left"]):
+        ref[:, [12, 14]] = ref[:, [14, 12]]
+    np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))

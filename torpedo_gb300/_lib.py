@@ -37,7 +37,10 @@ class Settings(C.Structure):
         ("depth_sort_items", C.c_uint32),
         ("sort_threads", C.c_uint32),
         ("depth_sort_threads", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("blend_round", C.c_uint32),
+        ("blend_backward_round", C.c_uint32),
+        ("blend_persistent", C.c_uint32),
+        ("reserved", C.c_uint32 * 3),
     ]
 
 

@@ -16,6 +16,17 @@ result bit for bit unchanged:
   sort_ctas_per_sm   residency the 256 x 16-key pass kernel is compiled for
                      (2: 128 registers, no spills; 3: 80 registers)
 
+For a training step (forward + backward, TRAIN_AXES) the blend's settings:
+
+  blend_round           list entries the blend stages per round (its batch
+                        depth): 128, 64 or 256
+  blend_backward_round  the same for the blend adjoint: 64, 32 or 128
+  blend_persistent      one CTA per tile (0), or persistent CTAs taking
+                        (view, tile) items from a queue over all views (1)
+
+Forward images are bit for bit the same under every setting; the adjoint's
+gradients are sums of float atomics, whose order no setting fixes.
+
 The tile size stays 16x16 and the radix digit 8 bits: the tile size fixes
 the reference's key layout (tile id | depth), and a 13-bit tile id takes two
 passes at any digit width from 7 to 12 bits.
@@ -26,6 +37,7 @@ from typing import Callable
 
 AXES = (("sort_threads", (512, 256)), ("depth_sort_threads", (256, 512)), ("depth_sort_items", (16, 8)),
         ("sort_ctas_per_sm", (2, 3)))
+TRAIN_AXES = (("blend_backward_round", (64, 32, 128)), ("blend_round", (128, 64, 256)), ("blend_persistent", (0, 1)))
 
 
 def time_steps(make_engine: Callable[[dict], object], enqueue: Callable[[object, int], None], stream,
@@ -48,17 +60,18 @@ def time_steps(make_engine: Callable[[dict], object], enqueue: Callable[[object,
 
 
 def tune(make_engine: Callable[[dict], object], enqueue: Callable[[object, int], None], stream,
-         frames: int = 20, warmup: int = 3, axes=AXES) -> tuple[dict, dict]:
+         frames: int = 20, warmup: int = 3, axes=AXES, base: dict | None = None) -> tuple[dict, dict]:
     """make_engine(settings) -> a ready engine (compiled, views set, one frame
     rendered); enqueue(engine, count) enqueues count steps on `stream` (a
-    torch.cuda.Stream). Returns (best settings, {label: ms per step})."""
-    best = {name: values[0] for name, values in axes}
+    torch.cuda.Stream). base: settings kept as they are. Returns (best
+    settings, {label: ms per step})."""
+    best = dict(base or {}, **{name: values[0] for name, values in axes})
     results: dict[str, float] = {}
     best_ms = None
     for name, values in axes:
         for v in values:
             cand = dict(best, **{name: v})
-            label = ",".join(f"{k}={x}" for k, x in cand.items())
+            label = ",".join(f"{k}={x}" for k, x in cand.items() if k in dict(axes))
             if label not in results:
                 results[label] = round(time_steps(make_engine, enqueue, stream, cand, frames, warmup), 4)
             if best_ms is None or results[label] < best_ms:

@@ -32,6 +32,8 @@
 // culled pair lies outside that ellipse, where the pair's own test finds
 // alpha below 1/255 and skips it, as the reference does; so the culling
 // changes which skipped pairs are visited, never a result.
+#include <algorithm>
+
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
 
@@ -154,11 +156,11 @@ __device__ __forceinline__ void load_view_tile(const ViewConst* views, const uin
 // holds its values duplicated in register-pair order, so the packed operands
 // come straight out of five broadcast shared-memory loads.
 constexpr uint32_t kFwdThreads = 128;
-// 128 list entries per staged round (20 KB of shared memory) and at most 64
-// registers: 8 CTAs (32 warps) per SM, measured faster than 256-entry rounds
-// at 5 CTAs, 64-entry rounds, or 10 CTAs at 48 registers
-constexpr uint32_t kRound = 128;
-constexpr uint32_t kFwdMinBlocks = 8;
+// List entries per staged round (the blend's batch depth, an engine setting
+// the autotuner picks): 128 by default (20 KB of shared memory, 8 CTAs per
+// SM at 64 registers); 64 (8 CTAs) or 256 (41 KB, 5 CTAs).
+template <uint32_t kRound>
+constexpr int fwd_min_blocks() { return kRound >= 256 ? 5 : 8; }
 
 struct PairStaged {  // 80 bytes
     float4 xy;       // x, x, y, y
@@ -168,6 +170,7 @@ struct PairStaged {  // 80 bytes
     float4 bt;       // b, b, thr, 0
 };
 
+template <uint32_t kRound>
 struct FwdStage {
     PairStaged e[2][kRound];
     uint8_t mask[2][kRound];  // bit w: the entry can reach warp w's 8x8 block
@@ -192,16 +195,13 @@ __device__ __forceinline__ void stage_pair_empty(PairStaged& d, uint8_t& mask) {
     mask = 0u;
 }
 
-// Rounds of kRound list entries, double-buffered: while the warps walk round
-// r, each thread stages its entry of round r + 1 into the other buffer, and
-// one barrier per round (which also counts finished pixels) separates the
-// two.
-__global__ void __launch_bounds__(kFwdThreads, kFwdMinBlocks) blend_kernel(BlendArgs a) {
-    __shared__ FwdStage S;
-
-    const uint32_t tile = blockIdx.x;
-    // an overflowed frame is re-rendered with larger key buffers; nothing to draw
-    if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
+// One tile: rounds of kRound list entries, double-buffered: while the warps
+// walk round r, each thread stages its entry of round r + 1 into the other
+// buffer, and one barrier per round (which also counts finished pixels)
+// separates the two. Called by the whole CTA; the first barrier comes after
+// the first staging and the last one after every read of S.
+template <uint32_t kRound>
+__device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, FwdStage<kRound>& S) {
     uint32_t vi, W, H, tx, ty;
     load_view_tile(a.views, a.tile_view, tile, vi, W, H, tx, ty);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -308,6 +308,37 @@ __global__ void __launch_bounds__(kFwdThreads, kFwdMinBlocks) blend_kernel(Blend
     }
 }
 
+// The tile scheduler of a persistent launch: the CTA takes the next item of
+// the frame's tile queue (an atomic ticket in FrameCtl) until the queue is
+// empty; item i is tile order[i] (nullptr: tile i). Every tile of every view
+// is one item, so one launch balances all views' tiles at once.
+__device__ __forceinline__ bool next_tile(FrameCtl* ctl, uint32_t slot, const uint32_t* order, uint32_t n_tiles,
+                                          uint32_t& tile) {
+    __shared__ uint32_t s_item;
+    if (threadIdx.x == 0) s_item = atomicAdd(&ctl->ticket[slot], 1u);
+    __syncthreads();
+    const uint32_t i = s_item;
+    __syncthreads();  // every thread has read s_item before it is written again
+    if (i >= n_tiles) return false;
+    tile = order ? order[i] : i;
+    return true;
+}
+
+// One CTA per tile, or (kPersistent) one CTA per resident slot taking tiles
+// from the queue.
+template <uint32_t kRound, bool kPersistent>
+__global__ void __launch_bounds__(kFwdThreads, fwd_min_blocks<kRound>()) blend_kernel(BlendArgs a) {
+    __shared__ FwdStage<kRound> S;
+    // an overflowed frame is re-rendered with larger key buffers; nothing to draw
+    if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
+    if constexpr (kPersistent) {
+        uint32_t tile;
+        while (next_tile(a.ctl, kTicketBlend, nullptr, a.n_tiles, tile)) blend_tile<kRound>(a, tile, S);
+    } else {
+        blend_tile<kRound>(a, blockIdx.x, S);
+    }
+}
+
 // UNORM conversion of (r, g, b, 1): round(clamp(c, 0, 1) * 255).
 __global__ void pack_rgba8_kernel(const float* rgb, uint32_t* rgba, size_t pixels) {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -362,10 +393,12 @@ __device__ __forceinline__ float warp_sum8_transposed(const float (&v)[8], uint3
 // reads live in three buffers (the next round's staging overwrites the one of
 // the round before the last).
 //
-// 64 list entries per round (17 KB of shared memory) and at most 64 registers:
-// 8 CTAs per SM; 128-entry rounds at 6 or 7 CTAs per SM measured the same
-constexpr uint32_t kBwdRound = 64;
-constexpr uint32_t kBwdMinBlocks = 8;
+// List entries per round (an engine setting the autotuner picks): 64 by
+// default (17 KB of shared memory, 8 CTAs per SM at 64 registers); 32 (8 CTAs)
+// or 128 (35 KB, 6 CTAs).
+template <uint32_t kBwdRound>
+constexpr int bwd_min_blocks() { return kBwdRound >= 128 ? 6 : 8; }
+template <uint32_t kBwdRound>
 struct BlendBackwardSmem {
     PairStaged e[2][kBwdRound];
     uint8_t mask[2][kBwdRound];
@@ -376,13 +409,11 @@ struct BlendBackwardSmem {
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-__global__ void __launch_bounds__(kFwdThreads, kBwdMinBlocks) blend_backward_kernel(BlendBackwardArgs a) {
-    extern __shared__ __align__(16) unsigned char bwd_smem[];
-    BlendBackwardSmem& SM = *reinterpret_cast<BlendBackwardSmem*>(bwd_smem);
-
-    const uint32_t tile = a.tile_order ? a.tile_order[blockIdx.x] : blockIdx.x;
-    if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
-    if (!TPD_INBOUNDS(a.ctl, 44, tile, a.n_tiles)) return;
+// One tile of the adjoint (the whole CTA; barriers as in blend_tile).
+template <uint32_t kBwdRound>
+__device__ __forceinline__ void blend_backward_tile(const BlendBackwardArgs& a, uint32_t tile,
+                                                    BlendBackwardSmem<kBwdRound>& SM) {
+    if (!TPD_INBOUNDS(a.ctl, 44, tile, a.n_tiles)) return;  // (uniform)
     uint32_t vi, W, H, tx, ty;
     load_view_tile(a.views, a.tile_view, tile, vi, W, H, tx, ty);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -535,6 +566,23 @@ __global__ void __launch_bounds__(kFwdThreads, kBwdMinBlocks) blend_backward_ker
             }
         }
     }
+    __syncthreads();  // the flush of the last round is done before SM is used again
+}
+
+// One CTA per tile, tile order[b] for CTA b; or (kPersistent) one CTA per
+// resident slot taking the tiles from the queue in that order.
+template <uint32_t kBwdRound, bool kPersistent>
+__global__ void __launch_bounds__(kFwdThreads, bwd_min_blocks<kBwdRound>())
+    blend_backward_kernel(BlendBackwardArgs a) {
+    __shared__ __align__(16) BlendBackwardSmem<kBwdRound> SM;
+    if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
+    if constexpr (kPersistent) {
+        uint32_t tile;
+        while (next_tile(a.ctl, kTicketBlendBackward, a.tile_order, a.n_tiles, tile))
+            blend_backward_tile<kBwdRound>(a, tile, SM);
+    } else {
+        blend_backward_tile<kBwdRound>(a, a.tile_order ? a.tile_order[blockIdx.x] : blockIdx.x, SM);
+    }
 }
 
 // One CTA: a counting sort of the tiles into 32 classes of list length
@@ -542,11 +590,12 @@ __global__ void __launch_bounds__(kFwdThreads, kBwdMinBlocks) blend_backward_ker
 constexpr uint32_t kOrderThreads = 1024;
 
 __global__ void __launch_bounds__(kOrderThreads)
-    tile_order_kernel(const uint32_t* __restrict__ ranges, uint32_t n_tiles, const FrameCtl* __restrict__ ctl,
+    tile_order_kernel(const uint32_t* __restrict__ ranges, uint32_t n_tiles, FrameCtl* __restrict__ ctl,
                       uint32_t capacity, uint32_t* __restrict__ order) {
     __shared__ uint32_t count[32], base[32];
     const uint32_t tid = threadIdx.x;
     if (tid < 32) count[tid] = 0;
+    if (tid == 0) ctl->ticket[kTicketBlendBackward] = 0;  // the adjoint's tile queue starts again
     __syncthreads();
     const uint32_t K = min(ctl->total_keys, capacity);
     // class c = floor(log2(len + 1)) in 0..31; slot 31 - c puts long lists first
@@ -574,15 +623,49 @@ __global__ void __launch_bounds__(kOrderThreads)
 
 }  // namespace
 
-void launch_tile_order(const uint32_t* ranges, uint32_t n_tiles, const FrameCtl* ctl, uint32_t capacity,
+void launch_tile_order(const uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, uint32_t capacity,
                        uint32_t* order, cudaStream_t s) {
     if (n_tiles == 0) return;
     tile_order_kernel<<<1, kOrderThreads, 0, s>>>(ranges, n_tiles, ctl, capacity, order);
 }
 
-void launch_blend(const BlendArgs& a, cudaStream_t s) {
+namespace {
+
+template <typename Kernel>
+int resident_ctas(Kernel k) {
+    int r = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k, kFwdThreads, 0);
+    return r > 0 ? r : 1;
+}
+template <uint32_t R, bool P>
+int blend_occupancy() { return resident_ctas(blend_kernel<R, P>); }
+template <uint32_t R, bool P>
+int blend_backward_occupancy() { return resident_ctas(blend_backward_kernel<R, P>); }
+
+template <uint32_t R, bool P>
+void launch_blend_t(const BlendArgs& a, int num_sms, cudaStream_t s) {
+    const uint32_t grid =
+        P ? std::min<uint32_t>(a.n_tiles, uint32_t(num_sms * device_once(blend_occupancy<R, P>))) : a.n_tiles;
+    blend_kernel<R, P><<<grid, kFwdThreads, 0, s>>>(a);
+}
+
+template <uint32_t R, bool P>
+void launch_blend_backward_t(const BlendBackwardArgs& a, int num_sms, cudaStream_t s) {
+    const uint32_t grid = P ? std::min<uint32_t>(a.n_tiles, uint32_t(num_sms * device_once(blend_backward_occupancy<R, P>)))
+                            : a.n_tiles;
+    blend_backward_kernel<R, P><<<grid, kFwdThreads, 0, s>>>(a);
+}
+
+}  // namespace
+
+void launch_blend(const BlendArgs& a, const BlendLaunch& l, cudaStream_t s) {
     if (a.n_tiles == 0) return;
-    blend_kernel<<<a.n_tiles, kFwdThreads, 0, s>>>(a);
+    const int sms = l.num_sms > 0 ? l.num_sms : 148;
+    switch (l.round) {
+        case 64: l.persistent ? launch_blend_t<64, true>(a, sms, s) : launch_blend_t<64, false>(a, sms, s); break;
+        case 256: l.persistent ? launch_blend_t<256, true>(a, sms, s) : launch_blend_t<256, false>(a, sms, s); break;
+        default: l.persistent ? launch_blend_t<128, true>(a, sms, s) : launch_blend_t<128, false>(a, sms, s); break;
+    }
 }
 
 void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStream_t s) {
@@ -590,19 +673,21 @@ void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStre
     pack_rgba8_kernel<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(rgb, rgba, pixels);
 }
 
-namespace {
-// more than 48 KB of shared memory needs the opt-in, on every device
-int blend_backward_setup() {
-    cudaFuncSetAttribute(blend_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(sizeof(BlendBackwardSmem)));
-    return 1;
-}
-}  // namespace
-
-void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s) {
+void launch_blend_backward(const BlendBackwardArgs& a, const BlendLaunch& l, cudaStream_t s) {
     if (a.n_tiles == 0) return;
-    device_once(blend_backward_setup);
-    blend_backward_kernel<<<a.n_tiles, kFwdThreads, sizeof(BlendBackwardSmem), s>>>(a);
+    const int sms = l.num_sms > 0 ? l.num_sms : 148;
+    switch (l.backward_round) {
+        case 32:
+            l.persistent ? launch_blend_backward_t<32, true>(a, sms, s) : launch_blend_backward_t<32, false>(a, sms, s);
+            break;
+        case 128:
+            l.persistent ? launch_blend_backward_t<128, true>(a, sms, s)
+                         : launch_blend_backward_t<128, false>(a, sms, s);
+            break;
+        default:
+            l.persistent ? launch_blend_backward_t<64, true>(a, sms, s) : launch_blend_backward_t<64, false>(a, sms, s);
+            break;
+    }
 }
 
 }  // namespace tpd

@@ -314,6 +314,18 @@ void harvest_all(tpd_engine* e) {
     for (int i = 0; i < tpd_engine::kTimingSlots; ++i) harvest_slot(e, i);
 }
 
+// The blend's launch settings (tpd_settings: round sizes and the persistent form).
+BlendLaunch blend_launch(const tpd_engine* e) {
+    BlendLaunch l;
+    l.round = e->settings.blend_round == 64 || e->settings.blend_round == 256 ? e->settings.blend_round : 128;
+    l.backward_round = e->settings.blend_backward_round == 32 || e->settings.blend_backward_round == 128
+                           ? e->settings.blend_backward_round
+                           : 64;
+    l.persistent = e->settings.blend_persistent != 0;
+    l.num_sms = e->num_sms;
+    return l;
+}
+
 // Enqueues one frame on the stream (no host synchronisation).
 // io = false leaves out the uploads of the view constants and transforms and
 // the stats copy (the pipelined renders enqueue those per slot).
@@ -430,7 +442,7 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     ba.image_offset = e->n_views > 1 ? e->d_image_offset : nullptr;
     ba.final_T = e->d_final_T;
     ba.n_contrib = e->d_n_contrib;
-    launch_blend(ba, s);
+    launch_blend(ba, blend_launch(e), s);
     mark(6);
     // the backward stages of a frame without backward take no time; a
     // training step records them again after its adjoint kernels
@@ -1075,7 +1087,7 @@ void enqueue_backward(tpd_engine* e, const float* dL_dimage, const BackwardOut& 
     launch_tile_order(e->d_ranges, e->total_tiles, e->d_ctl, uint32_t(e->capacity), e->d_tile_order, e->stream);
     bb.tile_order = e->d_tile_order;
     mark(TPD_STAGE_BACKWARD_SETUP + 1);
-    launch_blend_backward(bb, e->stream);
+    launch_blend_backward(bb, blend_launch(e), e->stream);
     mark(TPD_STAGE_BLEND_BACKWARD + 1);
     PreprocessBackwardArgs pb{};
     pb.recs = e->d_recs;

@@ -31,6 +31,8 @@ constexpr int kEntityMatFloats = 28;
 // Ticket slots and look-back tag slots (tag = ctl->tag * 32 + slot).
 constexpr int kTicketPreprocess = 0;
 constexpr int kTicketScan = 1;
+constexpr int kTicketBlend = 2;           // tile queue of a persistent blend launch
+constexpr int kTicketBlendBackward = 3;   // tile queue of a persistent adjoint launch (reset by tile order)
 constexpr int kTicketKeySortBase = 8;     // + 8-bit digit position
 constexpr int kTicketDepthSortBase = 16;  // + 8-bit digit position
 constexpr uint32_t kTagScan = 0;
@@ -165,7 +167,17 @@ struct BlendArgs {
     float* final_T;           // per pixel (nullable)
     uint32_t* n_contrib;      // per pixel (nullable)
 };
-void launch_blend(const BlendArgs& a, cudaStream_t s);
+// Launch settings of the blend and its adjoint: list entries per staged
+// round (forward 64 / 128 / 256, adjoint 32 / 64 / 128) and the form of the
+// launch: one CTA per tile, or persistent CTAs (SMs x resident CTAs) taking
+// (view, tile) items from a queue in FrameCtl. None of them changes a result.
+struct BlendLaunch {
+    uint32_t round = 128;
+    uint32_t backward_round = 64;
+    bool persistent = false;
+    int num_sms = 148;
+};
+void launch_blend(const BlendArgs& a, const BlendLaunch& l, cudaStream_t s);
 
 // RGBA8 UNORM pack of an HWC float3 image (alpha 1), the reference's target format.
 void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStream_t s);
@@ -189,14 +201,14 @@ struct BlendBackwardArgs {
     uint64_t g2d_view_stride; // floats between views' g2d (n * kG2DStride)
     const uint32_t* tile_order;  // nullable: CTA b differentiates tile tile_order[b] (launch_tile_order)
 };
-void launch_blend_backward(const BlendBackwardArgs& a, cudaStream_t s);
+void launch_blend_backward(const BlendBackwardArgs& a, const BlendLaunch& l, cudaStream_t s);
 
 // order[0 .. n_tiles): the tiles by decreasing list length (in classes of
 // equal floor(log2(length + 1)); any order within a class), so the longest
 // lists start first and no SM is left with one at the end. ranges as the
 // blend leaves them (empty tiles (0, 0)); lengths are clipped at
-// min(ctl->total_keys, capacity).
-void launch_tile_order(const uint32_t* ranges, uint32_t n_tiles, const FrameCtl* ctl, uint32_t capacity,
+// min(ctl->total_keys, capacity). Also resets the adjoint's tile queue.
+void launch_tile_order(const uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, uint32_t capacity,
                        uint32_t* order, cudaStream_t s);
 
 // Per-splat gradient record of the blend adjoint: 9 used floats padded to 12
