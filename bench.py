@@ -12,9 +12,10 @@ radix sort -> tile ranges -> blend, with the Gaussians resident in device memory
          uploaded from pinned host memory, the frame rendered and the RGBA8 image
          read back into pinned host memory (tpd_render_async / tpd_wait_render,
          two frames in flight)
-  roofline  the onesweep radix pass kernel of the key sort: algorithmic bytes
-         K*24 per launch over its average duration, from CUDA events recorded
-         between stages during a second timed region
+  roofline  one radix pass of the key sort (its counting and scatter kernels,
+         or its onesweep kernel): algorithmic bytes K*24 per pass over the
+         pass's average duration, from CUDA events recorded between stages
+         during a second timed region
   general_sort  the standalone radix sort on the frame's keys in random order,
          all key bits, sort GB/s by the fixed formula K*(8 + 24*ceil(B/8))
   cpu_baseline  the oracle's FP32 transcription of the reference shaders (same
@@ -533,11 +534,17 @@ def run_ours(args):
     sort_formula = K * (8 + 24 * math.ceil(key_bits / 8))
     pass_ms = stage_avg["key_sort"] / passes
     achieved = K * 24 / (pass_ms / 1000.0) / 1e9
+    # DRAM bytes per key of one pass, from the committed ncu capture of the
+    # pass's kernels (read + write), times K
+    counted = not settings.get("key_sort_lookback")
     traffic = None
-    tfile = ROOT / "profiles" / "onesweep_traffic.json"
+    tfile = ROOT / "profiles" / "radix_pass_traffic.json"
     if tfile.exists():
         t = json.loads(tfile.read_text())
-        traffic = int(t["dram_bytes_per_key"] * K)
+        per_key = t.get("counted" if counted else "onesweep")
+        traffic = int(per_key * K) if per_key else None
+    pass_kernel = ("partition_count_kernel + scatter_kernel (one counted 8-bit tile-id radix pass of the key sort)"
+                   if counted else "onesweep_kernel (one 8-bit tile-id radix pass of the key sort)")
     general = general_sort(eng, K, key_bits, stream, args.steps) if not args.no_general_sort else None
     eng.close()
 
@@ -595,7 +602,7 @@ def run_ours(args):
         "warmup": max(3, args.warmup), "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded cfg1 generator)",
         "config": workload_config(cfg, cam.width, cam.height, K),
-        "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit tile-id radix pass of the key sort)",
+        "roofline": {"bound": "hbm", "kernel": pass_kernel,
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_kind": f"{peak_kind} copy bandwidth",
                      "bytes_per_launch": K * 24, "avg_launch_ms": round(pass_ms, 5),

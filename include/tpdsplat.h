@@ -73,7 +73,8 @@ typedef struct tpd_settings {
     double timeout_s;              /* host wait limit per frame in seconds (0: 60) */
     uint32_t test_never_publish;   /* test hook: scan partition 0 never publishes (exercises the bounded spin) */
     uint32_t stage_timing;         /* 1: frames run without a graph and record CUDA events between stages */
-    uint32_t sort_ctas_per_sm;     /* residency of the 256 x 16-key radix pass kernel: 2 (0 = default, no register spills) or 3 */
+    uint32_t sort_ctas_per_sm;     /* residency of the 256 x 16-key radix pass kernels: 2 (0 = default, no register spills) or 3;
+                                      for the counted key sort 3 (0 = default) or 2 */
     uint32_t depth_sort_items;     /* keys per thread of the depth sort's 256-thread radix passes: 16 (0 = default), 8 or 4 */
     uint32_t sort_threads;         /* CTA size of the key sort's 4096-key radix passes: 512 x 8 keys (0 = default) or 256 x 16 */
     uint32_t depth_sort_threads;   /* CTA size of the depth sort's radix passes: 256 (0 = default) or 512 (8 keys each,
@@ -82,7 +83,10 @@ typedef struct tpd_settings {
     uint32_t blend_backward_round; /* list entries the blend adjoint stages per round: 64 (0 = default), 32 or 128 */
     uint32_t blend_persistent;     /* 1: the blend and its adjoint run persistent CTAs taking (view, tile) items from a
                                       queue (the adjoint's longest lists first); 0 (default): one CTA per tile */
-    uint32_t reserved[3];
+    uint32_t key_sort_lookback;    /* 0 (default): the key sort's radix passes count every partition's digits first and
+                                      scatter without waiting (counted passes, 3 CTAs per SM, or 2 with
+                                      sort_ctas_per_sm = 2); 1: onesweep passes with a decoupled look-back */
+    uint32_t reserved[2];
 } tpd_settings;
 
 /* Stages of a frame (and of a training step), for tpd_stage_times. */

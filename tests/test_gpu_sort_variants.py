@@ -1,9 +1,11 @@
 """Every radix pass variant gives the same frame, bit for bit.
 
-The engine settings sort_threads, depth_sort_threads, depth_sort_items and
-sort_ctas_per_sm choose among five compiled onesweep kernels (512 x 8 keys
-with match-any ranking; 256 x 16 keys at 2 or 3 CTAs per SM, 256 x 8 and
-256 x 4 keys with bit-ballot ranking) for the depth presort and the key sort.
+The engine settings key_sort_lookback, sort_threads, depth_sort_threads,
+depth_sort_items and sort_ctas_per_sm choose the key sort's form (counted
+passes at 3 or 2 CTAs per SM, or onesweep passes with a look-back) and
+among five compiled onesweep kernels (512 x 8 keys with match-any ranking;
+256 x 16 keys at 2 or 3 CTAs per SM, 256 x 8 and 256 x 4 keys with
+bit-ballot ranking) for the depth presort and the onesweep key sort.
 The default settings are checked against the oracle stage by stage in
 test_gpu_pipeline.py; here each other choice must reproduce the default
 frame exactly: sorted keys and values, tile ranges, image, final
@@ -19,8 +21,10 @@ from torpedo_gb300 import configs
 pytestmark = pytest.mark.gpu
 
 VARIANTS = [
-    dict(sort_threads=256),
-    dict(sort_threads=256, sort_ctas_per_sm=3),
+    dict(sort_ctas_per_sm=2),
+    dict(key_sort_lookback=True),
+    dict(key_sort_lookback=True, sort_threads=256),
+    dict(key_sort_lookback=True, sort_threads=256, sort_ctas_per_sm=3),
     dict(depth_sort_threads=512),
     dict(depth_sort_items=8),
     dict(depth_sort_items=4),

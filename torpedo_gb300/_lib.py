@@ -40,7 +40,8 @@ class Settings(C.Structure):
         ("blend_round", C.c_uint32),
         ("blend_backward_round", C.c_uint32),
         ("blend_persistent", C.c_uint32),
-        ("reserved", C.c_uint32 * 3),
+        ("key_sort_lookback", C.c_uint32),
+        ("reserved", C.c_uint32 * 2),
     ]
 
 

@@ -6,15 +6,20 @@ fastest, one axis at a time (each axis tried with the best values found so
 far for the others). The tunables are engine settings that leave every
 result bit for bit unchanged:
 
-  sort_threads       CTA size of the key sort's 4096-key radix passes: 512
+  key_sort_lookback  the key sort's radix passes: counted (0: every
+                     partition's digits counted and scanned first, then a
+                     scatter that waits for no other partition) or onesweep
+                     with a decoupled look-back (1)
+  sort_threads       CTA size of the onesweep key sort's 4096-key passes: 512
                      threads x 8 keys (digits ranked with match-any, twice the
                      warps per SM) or 256 threads x 16 keys (bit ballots)
   depth_sort_threads the same choice for the depth sort's passes
   depth_sort_items   keys per thread of the depth sort's 256-thread passes
                      (16, 8, 4: partitions of 4096, 2048, 1024 keys); smaller
                      partitions fill the GPU when the Gaussians are few
-  sort_ctas_per_sm   residency the 256 x 16-key pass kernel is compiled for
-                     (2: 128 registers, no spills; 3: 80 registers)
+  sort_ctas_per_sm   residency the 256 x 16-key pass kernels are compiled
+                     for: 0 the defaults (counted scatter 3 CTAs per SM at 80
+                     registers, onesweep 2 at 128), 2 both at 2
 
 For a training step (forward + backward, TRAIN_AXES) the blend's settings:
 
@@ -35,8 +40,8 @@ from __future__ import annotations
 
 from typing import Callable
 
-AXES = (("sort_threads", (512, 256)), ("depth_sort_threads", (256, 512)), ("depth_sort_items", (16, 8)),
-        ("sort_ctas_per_sm", (2, 3)))
+AXES = (("key_sort_lookback", (0, 1)), ("sort_threads", (256, 512)), ("depth_sort_threads", (256, 512)),
+        ("depth_sort_items", (16, 8)), ("sort_ctas_per_sm", (0, 2)))
 TRAIN_AXES = (("blend_backward_round", (64, 32, 128)), ("blend_round", (128, 64, 256)), ("blend_persistent", (0, 1)))
 
 

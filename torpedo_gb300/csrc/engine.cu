@@ -128,6 +128,7 @@ struct tpd_engine {
     uint64_t keys64_cap = 0;
     uint32_t* d_vals[2] = {nullptr, nullptr};
     uint64_t* d_desc_sort = nullptr;
+    uint32_t* d_sort_work = nullptr;  // counted key-sort passes: partition counts and offsets (zero at rest)
     uint32_t* d_ranges = nullptr;
     uint64_t pixel_cap = 0, tile_cap = 0;
     float* d_image = nullptr;
@@ -267,6 +268,9 @@ int ensure_key_capacity(tpd_engine* e, uint64_t want) {
     const size_t entries = sort_desc_entries(uint32_t(want));
     TPD_CUDA(e, dalloc(e->d_desc_sort, entries));
     TPD_CUDA(e, cudaMemset(e->d_desc_sort, 0, entries * 8));
+    const size_t words = sort_counted_work_words(uint32_t(want));
+    TPD_CUDA(e, dalloc(e->d_sort_work, words));
+    TPD_CUDA(e, cudaMemset(e->d_sort_work, 0, words * 4));
     e->capacity = want;
     return TPD_OK;
 }
@@ -423,6 +427,11 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     kp.threads = e->settings.sort_threads == 256 ? 256 : 512;
     kp.ranges = e->d_ranges;  // the last pass writes the tile ranges
     kp.n_tiles = e->total_tiles;
+    // counted passes (default), or onesweep passes with a look-back
+    if (e->settings.key_sort_lookback == 0) {
+        kp.counted_work = e->d_sort_work;
+        kp.ctas_per_sm = e->settings.sort_ctas_per_sm == 2 ? 2 : 3;
+    }
     e->sorted_in_alt = launch_sort(e->d_tiles[0], e->d_vals[0], e->d_tiles[1], e->d_vals[1], cap, kp, e->d_desc_sort,
                                    e->d_ctl, spin, e->num_sms, s);
     mark(4);
@@ -723,6 +732,7 @@ void tpd_destroy(tpd_engine* e) {
         dfree(e->d_vals[b]);
     }
     dfree(e->d_desc_sort);
+    dfree(e->d_sort_work);
     dfree(e->d_keys64);
     dfree(e->d_ranges);
     dfree(e->d_image);
@@ -1259,7 +1269,10 @@ int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t*
     plan.key_bits = key_bits;
     plan.hist = ctl->sort_hist;
     plan.hist_ready = false;
-    plan.threads = 512;  // 512 threads x 8 keys per 4096-key partition: the faster variant on GB300
+    // 512 threads x 8 keys per 4096-key partition with a look-back: on 64-bit
+    // keys faster than the counted passes (0.85 against 1.06 ms for 9M keys
+    // of 45 bits), which serve the frame's 32-bit key sort
+    plan.threads = 512;
     const bool alt = launch_sort(keys, vals, keys_alt, vals_alt, n, plan, desc, ctl, kDefaultSpin, sms, s);
     *result_in_alt = alt ? 1 : 0;
     return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;

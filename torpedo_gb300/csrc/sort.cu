@@ -476,6 +476,243 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     }
 }
 
+// ---- counted passes: a radix pass without look-back
+//
+// The look-back of onesweep_kernel puts a wait on every partition's critical
+// path (measured on the key sort of 1M Gaussians at 1080p: 4.4 of 10.5 us per
+// partition, after load and rank 3.0, scan 0.4, write-out 2.6). A counted pass
+// computes every partition's digit offsets beforehand instead:
+//  1. partition_count_kernel, one CTA per 4096-key partition: the partition's
+//     digit counts (per-warp shared-memory counts) as a row of work[]. The
+//     last CTA of each chunk of kChunkParts partitions to finish (an atomic
+//     arrival count; nobody waits) scans the chunk's rows per digit in place
+//     into offsets within the chunk and writes the chunk's totals; the last
+//     chunk to finish scans the chunk totals, starting from the pass's global
+//     digit offsets, into each chunk's base. Arrival counts are reset by the
+//     CTA that finishes them, so the work area is zero at rest.
+//  2. scatter_kernel, one CTA per partition: load, rank (bit ballots, stable
+//     in warp-striped order), reorder in shared memory and write out at
+//     chunk base + offset within chunk, as onesweep_kernel does but with its
+//     offsets known: no partition waits for another.
+// The permutation is the same stable one.
+constexpr uint32_t kChunkParts = 32;
+
+// Layout of a counted pass's work area (u32 words), for P partitions:
+// [0, 256 P) rows of digit counts, then offsets within their chunk;
+// [256 P, 256 P + 256 C) chunk totals, then chunk bases (C chunks);
+// [256 (P + C), + C) chunk arrival counts; then one arrival count of chunks.
+__host__ __device__ inline size_t counted_chunks(uint32_t parts) { return (parts + kChunkParts - 1) / kChunkParts; }
+__host__ __device__ inline size_t counted_work_words(uint32_t parts) {
+    const size_t c = counted_chunks(parts);
+    return 256 * (size_t(parts) + c) + c + 1;
+}
+
+__device__ __forceinline__ uint32_t ld_cg_u32(const uint32_t* p) { return __ldcg(p); }
+
+template <int kItems, typename KeyT>
+__global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __restrict__ keys, uint32_t capacity,
+                                                              uint32_t pass, uint32_t shift, uint32_t bits,
+                                                              const uint32_t (*hist)[256], uint32_t fixed_count,
+                                                              uint32_t max_parts, uint32_t* __restrict__ work,
+                                                              FrameCtl* ctl, uint32_t abort_mask) {
+    constexpr uint32_t kTile = 256 * kItems;
+    __shared__ uint32_t hw[8][kRadix];  // per-warp counts
+    __shared__ uint32_t wsum[8];
+    __shared__ bool last;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t K = (ctl->status & abort_mask) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
+    const uint32_t nparts = min((K + kTile - 1) / kTile, max_parts);
+    const uint32_t part = blockIdx.x;
+    if (part >= nparts) return;  // (uniform)
+    const uint32_t mask = (1u << bits) - 1u;
+#pragma unroll
+    for (uint32_t w = 0; w < 8; ++w) hw[w][tid] = 0;
+    __syncthreads();
+    const uint32_t base = part * kTile, cnt = min(kTile, K - base);
+    KeyT k[kItems];
+#pragma unroll
+    for (uint32_t i = 0; i < kItems; ++i) {
+        const uint32_t idx = i * 256 + tid;
+        k[i] = idx < cnt ? keys[base + idx] : KeyT(0);
+    }
+    // 32 consecutive keys often share a digit (a Gaussian's row of tiles, in
+    // the high digit): then one add of 32, else one shared atomic per key
+#pragma unroll
+    for (uint32_t i = 0; i < kItems; ++i) {
+        const uint32_t idx = i * 256 + tid;
+        const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
+        const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
+        if (__all_sync(0xFFFFFFFFu, d == d0)) {
+            if (lane == 0 && d < kRadix) hw[warp][d] += 32u;
+        } else if (d < kRadix) {
+            atomicAdd(&hw[warp][d], 1u);
+        }
+    }
+    __syncthreads();
+    uint32_t total = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < 8; ++w) total += hw[w][tid];
+    uint32_t* rows = work;
+    const uint32_t nchunks = uint32_t(counted_chunks(nparts));
+    uint32_t* chunk_rows = work + 256 * size_t(max_parts);
+    uint32_t* arrivals = chunk_rows + 256 * counted_chunks(max_parts);
+    rows[size_t(part) * 256 + tid] = total;
+    // the CTA's row is visible device-wide before its arrival is counted: the
+    // barrier orders every thread's store before thread 0's fence, which
+    // makes them visible with its own (a fence is cumulative); the last
+    // arriver's fence after its count orders its reads after all rows
+    __syncthreads();
+    const uint32_t chunk = part / kChunkParts;
+    const uint32_t first = chunk * kChunkParts, csize = min(kChunkParts, nparts - first);
+    if (tid == 0) {
+        __threadfence();
+        last = atomicAdd(&arrivals[chunk], 1u) == csize - 1u;
+        if (last) __threadfence();
+    }
+    __syncthreads();
+    if (!last) return;
+    // the chunk's last CTA: offsets within the chunk, in place, and its total
+    // (the chunk's rows are loaded together, then scanned)
+    uint32_t c[kChunkParts];
+#pragma unroll
+    for (uint32_t q = 0; q < kChunkParts; ++q)
+        c[q] = q < csize ? ld_cg_u32(rows + size_t(first + q) * 256 + tid) : 0u;
+    uint32_t run = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < kChunkParts; ++q) {
+        if (q < csize) rows[size_t(first + q) * 256 + tid] = run;
+        run += c[q];
+    }
+    chunk_rows[size_t(chunk) * 256 + tid] = run;
+    __syncthreads();
+    if (tid == 0) {
+        arrivals[chunk] = 0;
+        __threadfence();
+        last = atomicAdd(&arrivals[counted_chunks(max_parts)], 1u) == nchunks - 1u;
+        if (last) __threadfence();
+    }
+    __syncthreads();
+    if (!last) return;
+    // the last chunk: each chunk's base, from the pass's global digit offsets
+    const uint32_t hd = TPD_INBOUNDS(ctl, 19, pass, 8) ? hist[pass][tid] : 0u;
+    uint32_t gbase = block_exclusive_scan256<8>(hd, wsum);
+    for (uint32_t c0 = 0; c0 < nchunks; c0 += kChunkParts) {  // chunk totals, kChunkParts at a time
+#pragma unroll
+        for (uint32_t q = 0; q < kChunkParts; ++q)
+            c[q] = c0 + q < nchunks ? ld_cg_u32(chunk_rows + size_t(c0 + q) * 256 + tid) : 0u;
+#pragma unroll
+        for (uint32_t q = 0; q < kChunkParts; ++q) {
+            if (c0 + q < nchunks) chunk_rows[size_t(c0 + q) * 256 + tid] = gbase;
+            gbase += c[q];
+        }
+    }
+    if (tid == 0) arrivals[counted_chunks(max_parts)] = 0;
+}
+
+template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    scatter_kernel(const KeyT* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, KeyT* __restrict__ keys_out,
+                   uint32_t* __restrict__ vals_out, uint32_t capacity, uint32_t shift, uint32_t bits,
+                   uint32_t fixed_count, uint32_t max_parts, const uint32_t* __restrict__ work, FrameCtl* ctl,
+                   uint32_t* __restrict__ ranges, uint32_t n_tiles, uint32_t abort_mask) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr uint32_t kSortTile = kThreads * kItems, kWarps = kThreads / 32;
+    OnesweepSmem<kItems, kThreads, KeyT>& S = *reinterpret_cast<OnesweepSmem<kItems, kThreads, KeyT>*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const bool digit_thread = tid < kRadix;
+    const uint32_t K = (ctl->status & abort_mask) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
+    const uint32_t nparts = min((K + kSortTile - 1) / kSortTile, max_parts);
+    const uint32_t part = blockIdx.x;
+    if (part >= nparts) return;  // (uniform)
+    const uint32_t mask = (1u << bits) - 1u;
+    const uint32_t base = part * kSortTile, cnt = min(kSortTile, K - base);
+    KeyT k[kItems];
+    uint32_t vr[kItems];
+#pragma unroll
+    for (uint32_t i = 0; i < kItems; ++i) {
+        const uint32_t idx = warp * (kItems * 32) + i * 32 + lane;
+        k[i] = idx < cnt ? keys_in[base + idx] : KeyT(~KeyT(0));
+        vr[i] = idx < cnt ? vals_in[base + idx] : 0u;
+    }
+    // this partition's digit offsets: chunk base + offset within the chunk
+    uint32_t goff = 0;
+    if (digit_thread) {
+        const uint32_t* chunk_rows = work + 256 * size_t(max_parts);
+        goff = ld_cg_u32(chunk_rows + size_t(part / kChunkParts) * 256 + tid) +
+               ld_cg_u32(work + size_t(part) * 256 + tid);
+    }
+#pragma unroll
+    for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
+    __syncthreads();
+    // stable rank within the warp (warp-striped order): bit ballots
+    uint32_t dr[kItems];
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (uint32_t i = 0; i < kItems; ++i) {
+        const uint32_t idx = warp * (kItems * 32) + i * 32 + lane;
+        const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
+        uint32_t peers = 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t b = 0; b < kRadixBits; ++b) {
+            const bool on = (d >> b) & 1u;
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+            peers &= on ? bal : ~bal;
+        }
+        if (cnt < kSortTile) {
+            const bool on = d >= kRadix;
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+            peers &= on ? bal : ~bal;
+        }
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t prev = 0;
+        if (lane == leader && d < kRadix) {
+            prev = S.whist[warp][d];
+            S.whist[warp][d] = prev + __popc(peers);
+        }
+        prev = __shfl_sync(0xFFFFFFFFu, prev, leader);
+        dr[i] = d | ((prev + __popc(peers & lt)) << 9);
+        __syncwarp();
+    }
+    __syncthreads();
+    uint32_t count = 0;
+    if (digit_thread) {
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; ++w) {
+            const uint32_t c = S.whist[w][tid];
+            S.whist[w][tid] = count;
+            count += c;
+        }
+    }
+    const uint32_t lstart = block_exclusive_scan256<kWarps>(count, S.wsum);  // (its barriers cover whist)
+    if (digit_thread) {
+        S.lstart[tid] = lstart;
+        S.gmap[tid] = goff - lstart;
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t i = 0; i < kItems; ++i) {
+        const uint32_t d = dr[i] & 511u;
+        if (d < kRadix) {
+            const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+            if (TPD_INBOUNDS(ctl, 20, pos, cnt)) {
+                S.keys[pad16(pos)] = k[i];
+                S.vals[pad16(pos)] = vr[i];
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < cnt; j += kThreads) {
+        const KeyT key = S.keys[pad16(j)];
+        const uint32_t d = uint32_t(key >> shift) & mask;
+        const uint32_t g = S.gmap[d] + j;
+        if (g < capacity && TPD_INBOUNDS(ctl, 21, g, K + (K == 0))) {
+            keys_out[g] = key;
+            vals_out[g] = S.vals[pad16(j)];
+            if (ranges) tile_range_bounds(S, ranges, n_tiles, key, j, cnt, d, g, shift, mask, ctl);
+        }
+    }
+}
+
 // Residencies: the 256-thread, 16-key variant is compiled for 2 CTAs per SM
 // (128 registers, no spills; the default) or 3 (80 registers); the 512-thread,
 // 8-key variant for 2 (32 warps per SM); the 8- and 4-key 256-thread variants
@@ -531,7 +768,43 @@ void launch_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_
     }
 }
 
+template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+int scatter_setup() {
+    cudaFuncSetAttribute(scatter_kernel<kItems, kThreads, kMinBlocks, KeyT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(OnesweepSmem<kItems, kThreads, KeyT>)));
+    return 1;
+}
+
+// Counted passes (see partition_count_kernel): per pass a counting launch and
+// a scatter launch, one CTA per 4096-key partition each. work: the counted
+// work area (counted_work_words(max partitions) u32, zero at rest).
+template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+void launch_counted_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_t capacity, uint32_t p0,
+                           uint32_t p1, const SortPlan& plan, uint32_t (*hist)[256], uint32_t* work, FrameCtl* ctl,
+                           cudaStream_t s) {
+    static_assert(kThreads * kItems == 4096, "counted passes use 4096-key partitions");
+    device_once(scatter_setup<kItems, kThreads, kMinBlocks, KeyT>);
+    const size_t smem = sizeof(OnesweepSmem<kItems, kThreads, KeyT>);
+    const uint32_t max_parts = std::max(1u, (capacity + 4095u) / 4096u);
+    const uint32_t abort = kStatusFatal | (plan.skip_on_overflow ? kStatusKeyOverflow : 0u);
+    for (uint32_t p = p0; p < p1; ++p) {
+        const uint32_t shift = p * kRadixBits;
+        const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
+        partition_count_kernel<16, KeyT><<<max_parts, 256, 0, s>>>(kin, capacity, p, shift, bits, hist,
+                                                                   plan.fixed_count, max_parts, work, ctl, abort);
+        scatter_kernel<kItems, kThreads, kMinBlocks, KeyT><<<max_parts, kThreads, smem, s>>>(
+            kin, vin, kout, vout, capacity, shift, bits, plan.fixed_count, max_parts, work, ctl,
+            p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles, abort);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+}
+
 }  // namespace
+
+size_t sort_counted_work_words(uint32_t capacity) {
+    return counted_work_words(std::max(1u, (capacity + 4095u) / 4096u));
+}
 
 uint32_t sort_pass_count(uint32_t key_bits) { return (key_bits + kRadixBits - 1) / kRadixBits; }
 
@@ -557,6 +830,23 @@ bool launch_sort_t(KeyT* keys, uint32_t* vals, KeyT* keys_alt, uint32_t* vals_al
         sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, p0, p1, plan.key_bits, hist, ctl);
     }
     if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
+    if (plan.counted_work) {
+        if constexpr (sizeof(KeyT) == 4) {
+            if (plan.ctas_per_sm == 2)
+                launch_counted_passes<16, 256, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
+                                                  plan.counted_work, ctl, s);
+            else if (plan.ctas_per_sm == 4)
+                launch_counted_passes<16, 256, 4>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
+                                                  plan.counted_work, ctl, s);
+            else
+                launch_counted_passes<16, 256, 3>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
+                                                  plan.counted_work, ctl, s);
+        } else {
+            launch_counted_passes<16, 256, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
+                                              plan.counted_work, ctl, s);
+        }
+        return ((p1 - p0) & 1u) != 0;
+    }
     if (plan.threads == 512)
         launch_passes<8, 512, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,
                                  sms, s);

@@ -139,7 +139,13 @@ struct SortPlan {
     // passes sort; a later pass whose digit is the same for every key copies
     bool compact_culled = false;
     cudaEvent_t after_hist = nullptr;  // recorded between the histogram and the first pass
+    // non-null: counted passes (every partition's digit offsets counted and
+    // scanned beforehand, no look-back; plain pass kinds only) using this work
+    // area of sort_counted_work_words(capacity) u32, zero at rest (every
+    // launch leaves it so)
+    uint32_t* counted_work = nullptr;
 };
+size_t sort_counted_work_words(uint32_t capacity);
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
                  const SortPlan& plan, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, int num_sms,
                  cudaStream_t s);
