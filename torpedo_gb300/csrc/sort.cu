@@ -355,13 +355,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             if constexpr (kMatchRank) {
                 peers = __match_any_sync(0xFFFFFFFFu, d);
             } else {
-                // lanes with the same digit: one ballot per digit bit (bits
-                // above the pass's width are zero in every valid lane and
-                // leave the mask as it is), and one for the past-the-end (or
-                // dropped) digit in the partitions that can have any
+                // lanes with the same digit: one ballot per digit bit of the
+                // pass's width (bits above it are zero in every valid lane),
+                // and one for the past-the-end (or dropped) digit in the
+                // partitions that can have any
                 peers = 0xFFFFFFFFu;
 #pragma unroll
                 for (uint32_t b = 0; b < kRadixBits; ++b) {
+                    if (b >= bits) break;  // (uniform)
                     const bool on = (d >> b) & 1u;
                     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
                     peers &= on ? bal : ~bal;
@@ -654,6 +655,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         uint32_t peers = 0xFFFFFFFFu;
 #pragma unroll
         for (uint32_t b = 0; b < kRadixBits; ++b) {
+            if (b >= bits) break;  // (uniform) bits above the pass's width are 0 in every valid key
             const bool on = (d >> b) & 1u;
             const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
             peers &= on ? bal : ~bal;
@@ -834,9 +836,6 @@ bool launch_sort_t(KeyT* keys, uint32_t* vals, KeyT* keys_alt, uint32_t* vals_al
         if constexpr (sizeof(KeyT) == 4) {
             if (plan.ctas_per_sm == 2)
                 launch_counted_passes<16, 256, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
-                                                  plan.counted_work, ctl, s);
-            else if (plan.ctas_per_sm == 4)
-                launch_counted_passes<16, 256, 4>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
                                                   plan.counted_work, ctl, s);
             else
                 launch_counted_passes<16, 256, 3>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
