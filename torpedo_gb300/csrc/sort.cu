@@ -355,14 +355,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             if constexpr (kMatchRank) {
                 peers = __match_any_sync(0xFFFFFFFFu, d);
             } else {
-                // lanes with the same digit: one ballot per digit bit of the
-                // pass's width (bits above it are zero in every valid lane),
-                // and one for the past-the-end (or dropped) digit in the
-                // partitions that can have any
+                // lanes with the same digit: one ballot per digit bit (bits
+                // above the pass's width are zero in every valid lane and
+                // leave the mask as it is), and one for the past-the-end (or
+                // dropped) digit in the partitions that can have any
                 peers = 0xFFFFFFFFu;
 #pragma unroll
                 for (uint32_t b = 0; b < kRadixBits; ++b) {
-                    if (b >= bits) break;  // (uniform)
                     const bool on = (d >> b) & 1u;
                     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
                     peers &= on ? bal : ~bal;
@@ -610,7 +609,10 @@ __global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __rest
     if (tid == 0) arrivals[counted_chunks(max_parts)] = 0;
 }
 
-template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+// kBits: the pass's digit width (1..8); the lanes with the same digit are
+// found with one ballot per digit bit (the launch picks the variant of the
+// pass's width: a 5-bit pass ranks with 5 ballots, not 8).
+template <int kItems, int kThreads, int kMinBlocks, int kBits, typename KeyT>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     scatter_kernel(const KeyT* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, KeyT* __restrict__ keys_out,
                    uint32_t* __restrict__ vals_out, uint32_t capacity, uint32_t shift, uint32_t bits,
@@ -645,7 +647,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 #pragma unroll
     for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
     __syncthreads();
-    // stable rank within the warp (warp-striped order): bit ballots
+    // stable rank within the warp (warp-striped order)
     uint32_t dr[kItems];
     const uint32_t lt = lanemask_lt();
 #pragma unroll
@@ -654,8 +656,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
         uint32_t peers = 0xFFFFFFFFu;
 #pragma unroll
-        for (uint32_t b = 0; b < kRadixBits; ++b) {
-            if (b >= bits) break;  // (uniform) bits above the pass's width are 0 in every valid key
+        for (int b = 0; b < kBits; ++b) {
             const bool on = (d >> b) & 1u;
             const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
             peers &= on ? bal : ~bal;
@@ -770,11 +771,51 @@ void launch_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_
     }
 }
 
-template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+template <int kItems, int kThreads, int kMinBlocks, int kBits, typename KeyT>
 int scatter_setup() {
-    cudaFuncSetAttribute(scatter_kernel<kItems, kThreads, kMinBlocks, KeyT>,
+    cudaFuncSetAttribute(scatter_kernel<kItems, kThreads, kMinBlocks, kBits, KeyT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(OnesweepSmem<kItems, kThreads, KeyT>)));
     return 1;
+}
+
+// Counted passes (see partition_count_kernel): per pass a counting launch and
+// a scatter launch, one CTA per 4096-key partition each. work: the counted
+// work area (counted_work_words(max partitions) u32, zero at rest).
+template <int kItems, int kThreads, int kMinBlocks, int kBits, typename KeyT>
+void launch_scatter(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_t capacity, uint32_t shift,
+                    uint32_t bits, const SortPlan& plan, uint32_t max_parts, uint32_t* work, FrameCtl* ctl,
+                    uint32_t* ranges, uint32_t abort, cudaStream_t s) {
+    device_once(scatter_setup<kItems, kThreads, kMinBlocks, kBits, KeyT>);
+    scatter_kernel<kItems, kThreads, kMinBlocks, kBits, KeyT>
+        <<<max_parts, kThreads, sizeof(OnesweepSmem<kItems, kThreads, KeyT>), s>>>(
+            kin, vin, kout, vout, capacity, shift, bits, plan.fixed_count, max_parts, work, ctl, ranges, plan.n_tiles,
+            abort);
+}
+
+// The scatter of one pass of `bits` bits: ballots for exactly that width (the
+// 3-CTA variant; the 2-CTA one ranks with 8 ballots).
+template <int kItems, int kThreads, int kMinBlocks, typename KeyT>
+void launch_scatter_bits(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_t capacity, uint32_t shift,
+                         uint32_t bits, const SortPlan& plan, uint32_t max_parts, uint32_t* work, FrameCtl* ctl,
+                         uint32_t* ranges, uint32_t abort, cudaStream_t s) {
+#define TPD_SCATTER(R) \
+    launch_scatter<kItems, kThreads, kMinBlocks, R, KeyT>(kin, vin, kout, vout, capacity, shift, bits, plan, \
+                                                          max_parts, work, ctl, ranges, abort, s)
+    if constexpr (kMinBlocks != 3) {
+        TPD_SCATTER(8);
+    } else {
+        switch (bits) {
+            case 1: TPD_SCATTER(1); break;
+            case 2: TPD_SCATTER(2); break;
+            case 3: TPD_SCATTER(3); break;
+            case 4: TPD_SCATTER(4); break;
+            case 5: TPD_SCATTER(5); break;
+            case 6: TPD_SCATTER(6); break;
+            case 7: TPD_SCATTER(7); break;
+            default: TPD_SCATTER(8); break;
+        }
+    }
+#undef TPD_SCATTER
 }
 
 // Counted passes (see partition_count_kernel): per pass a counting launch and
@@ -785,8 +826,6 @@ void launch_counted_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout,
                            uint32_t p1, const SortPlan& plan, uint32_t (*hist)[256], uint32_t* work, FrameCtl* ctl,
                            cudaStream_t s) {
     static_assert(kThreads * kItems == 4096, "counted passes use 4096-key partitions");
-    device_once(scatter_setup<kItems, kThreads, kMinBlocks, KeyT>);
-    const size_t smem = sizeof(OnesweepSmem<kItems, kThreads, KeyT>);
     const uint32_t max_parts = std::max(1u, (capacity + 4095u) / 4096u);
     const uint32_t abort = kStatusFatal | (plan.skip_on_overflow ? kStatusKeyOverflow : 0u);
     for (uint32_t p = p0; p < p1; ++p) {
@@ -794,9 +833,9 @@ void launch_counted_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout,
         const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
         partition_count_kernel<16, KeyT><<<max_parts, 256, 0, s>>>(kin, capacity, p, shift, bits, hist,
                                                                    plan.fixed_count, max_parts, work, ctl, abort);
-        scatter_kernel<kItems, kThreads, kMinBlocks, KeyT><<<max_parts, kThreads, smem, s>>>(
-            kin, vin, kout, vout, capacity, shift, bits, plan.fixed_count, max_parts, work, ctl,
-            p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles, abort);
+        launch_scatter_bits<kItems, kThreads, kMinBlocks, KeyT>(kin, vin, kout, vout, capacity, shift, bits, plan,
+                                                                max_parts, work, ctl,
+                                                                p + 1 == p1 ? plan.ranges : nullptr, abort, s);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
@@ -832,19 +871,16 @@ bool launch_sort_t(KeyT* keys, uint32_t* vals, KeyT* keys_alt, uint32_t* vals_al
         sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, p0, p1, plan.key_bits, hist, ctl);
     }
     if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
-    if (plan.counted_work) {
-        if constexpr (sizeof(KeyT) == 4) {
+    if constexpr (sizeof(KeyT) == 4) {  // counted passes: 32-bit keys (for 64-bit keys onesweep is faster)
+        if (plan.counted_work) {
             if (plan.ctas_per_sm == 2)
                 launch_counted_passes<16, 256, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
                                                   plan.counted_work, ctl, s);
             else
                 launch_counted_passes<16, 256, 3>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
                                                   plan.counted_work, ctl, s);
-        } else {
-            launch_counted_passes<16, 256, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist,
-                                              plan.counted_work, ctl, s);
+            return ((p1 - p0) & 1u) != 0;
         }
-        return ((p1 - p0) & 1u) != 0;
     }
     if (plan.threads == 512)
         launch_passes<8, 512, 2>(keys, vals, keys_alt, vals_alt, capacity, p0, p1, plan, hist, desc, ctl, spin_limit,

@@ -139,8 +139,8 @@ struct SortPlan {
     // passes sort; a later pass whose digit is the same for every key copies
     bool compact_culled = false;
     cudaEvent_t after_hist = nullptr;  // recorded between the histogram and the first pass
-    // non-null: counted passes (every partition's digit offsets counted and
-    // scanned beforehand, no look-back; plain pass kinds only) using this work
+    // non-null, 32-bit keys: counted passes (every partition's digit offsets
+    // counted and scanned beforehand, no look-back; plain pass kinds only) using this work
     // area of sort_counted_work_words(capacity) u32, zero at rest (every
     // launch leaves it so)
     uint32_t* counted_work = nullptr;
