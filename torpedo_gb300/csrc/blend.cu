@@ -329,6 +329,7 @@ __device__ __forceinline__ bool next_tile(FrameCtl* ctl, uint32_t slot, const ui
 template <uint32_t kRound, bool kPersistent>
 __global__ void __launch_bounds__(kFwdThreads, fwd_min_blocks<kRound>()) blend_kernel(BlendArgs a) {
     __shared__ FwdStage<kRound> S;
+    pdl_wait();  // launched as a dependent of the key sort's last pass: its lists and ranges
     // an overflowed frame is re-rendered with larger key buffers; nothing to draw
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
     if constexpr (kPersistent) {
@@ -646,7 +647,7 @@ template <uint32_t R, bool P>
 void launch_blend_t(const BlendArgs& a, int num_sms, cudaStream_t s) {
     const uint32_t grid =
         P ? std::min<uint32_t>(a.n_tiles, uint32_t(num_sms * device_once(blend_occupancy<R, P>))) : a.n_tiles;
-    blend_kernel<R, P><<<grid, kFwdThreads, 0, s>>>(a);
+    launch_dependent(blend_kernel<R, P>, dim3(grid), dim3(kFwdThreads), 0, s, a);
 }
 
 template <uint32_t R, bool P>

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
                   uint32_t capacity, uint32_t key_bits, uint32_t* __restrict__ ranges, uint32_t n_tiles,
                   FrameCtl* ctl) {
     __shared__ KeygenSmem S;
+    pdl_trigger();  // the key sort's first counting kernel may be scheduled (it waits for this grid)
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     const uint32_t warps_total = (gridDim.x * blockDim.x) >> 5;
     const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

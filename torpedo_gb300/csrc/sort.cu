@@ -520,6 +520,12 @@ __global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __rest
     __shared__ uint32_t wsum[8];
     __shared__ bool last;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    // launched as a dependent of the kernel that wrote the keys: wait for it,
+    // then let the scatter be scheduled (it loads its keys and values while
+    // the last partitions are counted; they come from the kernel this one
+    // waited for)
+    pdl_wait();
+    pdl_trigger();
     const uint32_t K = (ctl->status & abort_mask) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
     const uint32_t nparts = min((K + kTile - 1) / kTile, max_parts);
     const uint32_t part = blockIdx.x;
@@ -637,7 +643,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         k[i] = idx < cnt ? keys_in[base + idx] : KeyT(~KeyT(0));
         vr[i] = idx < cnt ? vals_in[base + idx] : 0u;
     }
-    // this partition's digit offsets: chunk base + offset within the chunk
+    // this partition's digit offsets: chunk base + offset within the chunk,
+    // written by the counting kernel (this kernel may have started while it
+    // ran: its keys and values come from the kernel before that one)
+    pdl_wait();
+    pdl_trigger();  // the next kernel (the next counting kernel, or the blend) may be scheduled; it waits for this grid
     uint32_t goff = 0;
     if (digit_thread) {
         const uint32_t* chunk_rows = work + 256 * size_t(max_parts);
@@ -786,10 +796,9 @@ void launch_scatter(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32
                     uint32_t bits, const SortPlan& plan, uint32_t max_parts, uint32_t* work, FrameCtl* ctl,
                     uint32_t* ranges, uint32_t abort, cudaStream_t s) {
     device_once(scatter_setup<kItems, kThreads, kMinBlocks, kBits, KeyT>);
-    scatter_kernel<kItems, kThreads, kMinBlocks, kBits, KeyT>
-        <<<max_parts, kThreads, sizeof(OnesweepSmem<kItems, kThreads, KeyT>), s>>>(
-            kin, vin, kout, vout, capacity, shift, bits, plan.fixed_count, max_parts, work, ctl, ranges, plan.n_tiles,
-            abort);
+    launch_dependent(scatter_kernel<kItems, kThreads, kMinBlocks, kBits, KeyT>, dim3(max_parts), dim3(kThreads),
+                     sizeof(OnesweepSmem<kItems, kThreads, KeyT>), s, kin, vin, kout, vout, capacity, shift, bits,
+                     plan.fixed_count, max_parts, work, ctl, ranges, plan.n_tiles, abort);
 }
 
 // The scatter of one pass of `bits` bits: ballots for exactly that width (the
@@ -831,8 +840,9 @@ void launch_counted_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout,
     for (uint32_t p = p0; p < p1; ++p) {
         const uint32_t shift = p * kRadixBits;
         const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
-        partition_count_kernel<16, KeyT><<<max_parts, 256, 0, s>>>(kin, capacity, p, shift, bits, hist,
-                                                                   plan.fixed_count, max_parts, work, ctl, abort);
+        launch_dependent(partition_count_kernel<16, KeyT>, dim3(max_parts), dim3(256), 0, s, kin, capacity, p, shift,
+                         bits, static_cast<const uint32_t(*)[256]>(hist), plan.fixed_count, max_parts, work, ctl,
+                         abort);
         launch_scatter_bits<kItems, kThreads, kMinBlocks, KeyT>(kin, vin, kout, vout, capacity, shift, bits, plan,
                                                                 max_parts, work, ctl,
                                                                 p + 1 == p1 ? plan.ranges : nullptr, abort, s);

@@ -73,6 +73,35 @@ __device__ __forceinline__ void cp_async_wait_all_but_newest() { asm volatile("c
 // Every committed group of this thread has completed.
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// Programmatic dependent launch (launch_dependent below). pdl_trigger: this
+// CTA allows the stream's next kernel to be scheduled (once every CTA of this
+// grid has done so or exited, so all of them are resident by then).
+// pdl_wait: blocks until the grids this one depends on have completed and
+// their memory is visible (hardware-managed, like a kernel boundary); reads of
+// their results come after it. Both are no-ops in a kernel launched without
+// the attribute.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launches kernel on s as a programmatic dependent of the kernel before it on
+// the stream: it may start while that kernel's last CTAs run, and must
+// pdl_wait() before it reads what that kernel writes.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                    Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Relaxed, device-scope 64-bit load / store: single-copy atomic, used for
 // self-contained look-back descriptors (flag + tag + value in one word).
 __device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
