@@ -57,6 +57,8 @@ constexpr uint32_t kBwdThreads = 128;
 // SH gradients leave through the same buffer as coalesced 16-byte stores.
 __global__ void __launch_bounds__(kBwdThreads) preprocess_backward_kernel(PreprocessBackwardArgs a) {
     __shared__ __align__(16) float srec[kBwdThreads * kRecordFloats];  // 30 KB; reused for the SH gradients
+    pdl_wait();  // launched as a dependent of the stream's previous kernel: its output is read below
+    pdl_trigger();
     const uint32_t base = blockIdx.x * kBwdThreads;
     const uint32_t cnt = min(kBwdThreads, a.n - base);
     {
@@ -290,7 +292,8 @@ __global__ void __launch_bounds__(kBwdThreads) preprocess_backward_kernel(Prepro
 
 void launch_preprocess_backward(const PreprocessBackwardArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
-    preprocess_backward_kernel<<<(a.n + kBwdThreads - 1) / kBwdThreads, kBwdThreads, 0, s>>>(a);
+    launch_dependent(preprocess_backward_kernel, dim3((a.n + kBwdThreads - 1) / kBwdThreads), dim3(kBwdThreads), 0,
+                     s, a);
 }
 
 }  // namespace tpd

@@ -330,6 +330,7 @@ template <uint32_t kRound, bool kPersistent>
 __global__ void __launch_bounds__(kFwdThreads, fwd_min_blocks<kRound>()) blend_kernel(BlendArgs a) {
     __shared__ FwdStage<kRound> S;
     pdl_wait();  // launched as a dependent of the key sort's last pass: its lists and ranges
+    pdl_trigger();
     // an overflowed frame is re-rendered with larger key buffers; nothing to draw
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
     if constexpr (kPersistent) {
@@ -342,6 +343,8 @@ __global__ void __launch_bounds__(kFwdThreads, fwd_min_blocks<kRound>()) blend_k
 
 // UNORM conversion of (r, g, b, 1): round(clamp(c, 0, 1) * 255).
 __global__ void pack_rgba8_kernel(const float* rgb, uint32_t* rgba, size_t pixels) {
+    pdl_wait();  // launched as a dependent of the blend
+    pdl_trigger();
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= pixels) return;
     uint32_t out = 0xFF000000u;
@@ -576,6 +579,8 @@ template <uint32_t kBwdRound, bool kPersistent>
 __global__ void __launch_bounds__(kFwdThreads, bwd_min_blocks<kBwdRound>())
     blend_backward_kernel(BlendBackwardArgs a) {
     __shared__ __align__(16) BlendBackwardSmem<kBwdRound> SM;
+    pdl_wait();  // launched as a dependent of the stream's previous kernel: its output is read below
+    pdl_trigger();
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;  // no valid frame to differentiate
     if constexpr (kPersistent) {
         uint32_t tile;
@@ -594,6 +599,8 @@ __global__ void __launch_bounds__(kOrderThreads)
     tile_order_kernel(const uint32_t* __restrict__ ranges, uint32_t n_tiles, FrameCtl* __restrict__ ctl,
                       uint32_t capacity, uint32_t* __restrict__ order) {
     __shared__ uint32_t count[32], base[32];
+    pdl_wait();  // launched as a dependent of the stream's previous kernel: its output is read below
+    pdl_trigger();
     const uint32_t tid = threadIdx.x;
     if (tid < 32) count[tid] = 0;
     if (tid == 0) ctl->ticket[kTicketBlendBackward] = 0;  // the adjoint's tile queue starts again
@@ -627,7 +634,7 @@ __global__ void __launch_bounds__(kOrderThreads)
 void launch_tile_order(const uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, uint32_t capacity,
                        uint32_t* order, cudaStream_t s) {
     if (n_tiles == 0) return;
-    tile_order_kernel<<<1, kOrderThreads, 0, s>>>(ranges, n_tiles, ctl, capacity, order);
+    launch_dependent(tile_order_kernel, dim3(1), dim3(kOrderThreads), 0, s, ranges, n_tiles, ctl, capacity, order);
 }
 
 namespace {
@@ -647,14 +654,17 @@ template <uint32_t R, bool P>
 void launch_blend_t(const BlendArgs& a, int num_sms, cudaStream_t s) {
     const uint32_t grid =
         P ? std::min<uint32_t>(a.n_tiles, uint32_t(num_sms * device_once(blend_occupancy<R, P>))) : a.n_tiles;
-    launch_dependent(blend_kernel<R, P>, dim3(grid), dim3(kFwdThreads), 0, s, a);
+    if (P)  // a persistent grid is placed once: on SMs the key sort has left, not while its last CTAs run
+        blend_kernel<R, P><<<grid, kFwdThreads, 0, s>>>(a);
+    else
+        launch_dependent(blend_kernel<R, P>, dim3(grid), dim3(kFwdThreads), 0, s, a);
 }
 
 template <uint32_t R, bool P>
 void launch_blend_backward_t(const BlendBackwardArgs& a, int num_sms, cudaStream_t s) {
     const uint32_t grid = P ? std::min<uint32_t>(a.n_tiles, uint32_t(num_sms * device_once(blend_backward_occupancy<R, P>)))
                             : a.n_tiles;
-    blend_backward_kernel<R, P><<<grid, kFwdThreads, 0, s>>>(a);
+    launch_dependent(blend_backward_kernel<R, P>, dim3(grid), dim3(kFwdThreads), 0, s, a);
 }
 
 }  // namespace
@@ -671,7 +681,8 @@ void launch_blend(const BlendArgs& a, const BlendLaunch& l, cudaStream_t s) {
 
 void launch_pack_rgba8(const float* rgb, uint32_t* rgba, size_t pixels, cudaStream_t s) {
     if (pixels == 0) return;
-    pack_rgba8_kernel<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(rgb, rgba, pixels);
+    launch_dependent(pack_rgba8_kernel, dim3(unsigned((pixels + 255) / 256)), dim3(256), 0, s,
+                     static_cast<const float*>(rgb), rgba, pixels);
 }
 
 void launch_blend_backward(const BlendBackwardArgs& a, const BlendLaunch& l, cudaStream_t s) {

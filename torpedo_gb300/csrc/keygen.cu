@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
                   uint32_t capacity, uint32_t key_bits, uint32_t* __restrict__ ranges, uint32_t n_tiles,
                   FrameCtl* ctl) {
     __shared__ KeygenSmem S;
+    pdl_wait();     // launched as a dependent of the depth-order scan: its offsets are read below
     pdl_trigger();  // the key sort's first counting kernel may be scheduled (it waits for this grid)
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     const uint32_t warps_total = (gridDim.x * blockDim.x) >> 5;
@@ -205,8 +206,8 @@ void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* o
     const int per_sm = device_once(keygen_setup);  // resident CTAs per SM (shared memory bound)
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
     blocks = blocks < cap ? blocks : cap;
-    keygen_kernel<<<unsigned(blocks), kKeygenThreads, 0, s>>>(splats, items, offsets, n_items, n, views, tiles, vals,
-                                                              capacity, key_bits, ranges, n_tiles, ctl);
+    launch_dependent(keygen_kernel, dim3(unsigned(blocks)), dim3(kKeygenThreads), 0, s, splats, items, offsets,
+                     n_items, n, views, tiles, vals, capacity, key_bits, ranges, n_tiles, ctl);
 }
 
 namespace {

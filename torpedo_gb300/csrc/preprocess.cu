@@ -71,6 +71,7 @@ __device__ __forceinline__ void mat3T(const float* A, float* B) {
 // identical values since they do not depend on the Gaussian).
 __global__ void frame_begin_kernel(FrameCtl* ctl, const float* transforms, uint32_t n_ent, const ViewConst* views,
                                    uint32_t n_views, float* ent_mats) {
+    pdl_trigger();  // the preprocess may be scheduled; it waits for this kernel
     const uint32_t t = threadIdx.x;
     for (uint32_t i = t; i < 32; i += blockDim.x) ctl->ticket[i] = 0;
     for (uint32_t i = t; i < 8 * 256; i += blockDim.x) {
@@ -304,6 +305,10 @@ __global__ void __launch_bounds__(kPreThreads, 3) preprocess_kernel(PreprocessAr
     const uint32_t tid = threadIdx.x;
     for (uint32_t k = tid; k < kDepthPassesMax * 256; k += kPreThreads) (&S.hist[0][0])[k] = 0;
     for (uint32_t k = tid; k < 257; k += kPreThreads) S.tdiff[k] = 0;
+    // launched as a dependent of frame_begin_kernel (the frame's control block).
+    // No early trigger: the depth sort's first pass is one wave of CTAs, which
+    // must be placed on empty SMs, not onto the first ones this grid frees
+    pdl_wait();
     for (uint32_t k = tid; k < (kTileDigitsMax - 1) * 256; k += kPreThreads) (&S.thist[0][0])[k] = 0;
     if (tid == 0) S.tall = 0;
     const uint32_t ndig = min(kTileDigitsMax, (a.tile_bits + 7) / 8);  // 0: no tile-digit counts
@@ -449,6 +454,10 @@ __global__ void __launch_bounds__(kScanThreads)
                       FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish) {
     constexpr uint32_t kScanTile = kScanThreads * kItems;
     __shared__ uint32_t s_part, s_excl;
+    // launched as a dependent of the stream's previous kernel: its output is
+    // read below. No early trigger: the next kernel is one wave of CTAs, which
+    // must be placed on empty SMs, not onto the first ones this grid frees
+    pdl_wait();
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t n = kGather ? min(ctl->depth_count, n_max) : n_max;
@@ -553,7 +562,7 @@ void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s) {
     const int per_sm = device_once(preprocess_setup);
     const uint32_t chunks = (a.n + kPreThreads - 1) / kPreThreads;
     const uint32_t blocks = std::min<uint32_t>(chunks, uint32_t((num_sms > 0 ? num_sms : 148) * per_sm));
-    preprocess_kernel<<<blocks, kPreThreads, sizeof(PreSmem), s>>>(a);
+    launch_dependent(preprocess_kernel, dim3(blocks), dim3(kPreThreads), sizeof(PreSmem), s, a);
 }
 
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
@@ -568,8 +577,8 @@ void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t max_
                        uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
     if (max_count == 0) return;
     const uint32_t blocks = (max_count + kScanThreads * 16 - 1) / (kScanThreads * 16);
-    scan_tiles_kernel<true, 16><<<blocks, kScanThreads, 0, s>>>(splats, items, max_count, offsets, desc, ctl,
-                                                                spin_limit, never_publish);
+    launch_dependent(scan_tiles_kernel<true, 16>, dim3(blocks), dim3(kScanThreads), 0, s, splats, items, max_count,
+                     offsets, desc, ctl, spin_limit, never_publish);
 }
 
 void launch_pack_records(const float* means, const float* log_scales, const float* quats, const float* logits,

@@ -121,6 +121,10 @@ __global__ void __launch_bounds__(kHistThreads)
     sort_histogram_kernel(const KeyT* __restrict__ keys, uint32_t capacity, uint32_t p0, uint32_t p1,
                           uint32_t key_bits, uint32_t (*hist)[256], FrameCtl* ctl) {
     __shared__ uint32_t sh[8][kRadix];
+    // launched as a dependent of the stream's previous kernel: its output is
+    // read below. No early trigger: the next kernel is one wave of CTAs, which
+    // must be placed on empty SMs, not onto the first ones this grid frees
+    pdl_wait();
     const uint32_t tid = threadIdx.x;
     for (uint32_t i = tid; i < 8 * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
     __syncthreads();
@@ -265,6 +269,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     uint32_t spin_limit, uint32_t* __restrict__ ranges, uint32_t n_tiles, uint32_t abort_mask) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr uint32_t kSortItems = kItems, kSortTile = kThreads * kItems, kWarps = kThreads / 32;
+    // launched as a dependent of the stream's previous kernel: its output is
+    // read below. No early trigger: the next kernel is one wave of CTAs, which
+    // must be placed on empty SMs, not onto the first ones this grid frees
+    pdl_wait();
     // digits ranked with match-any in the 512-thread variant (32 warps per SM
     // hide its latency), with bit ballots otherwise (fixed cost)
     constexpr bool kMatchRank = kThreads == 512;
@@ -772,10 +780,10 @@ void launch_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout, uint32_
                 kernel = p == p0 ? onesweep_kernel<kItems, kThreads, kMinBlocks, kPassDropCulled, KeyT>
                                  : onesweep_kernel<kItems, kThreads, kMinBlocks, kPassCompacted, KeyT>;
         }
-        kernel<<<grid, kThreads, smem, s>>>(kin, vin, kout, vout, capacity, p, shift, bits, hist, plan.ticket_base + p,
-                                            plan.tag_base + p, plan.fixed_count, desc, ctl, spin_limit,
-                                            p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles,
-                                            kStatusFatal | (plan.skip_on_overflow ? kStatusKeyOverflow : 0u));
+        launch_dependent(kernel, dim3(grid), dim3(kThreads), smem, s, kin, vin, kout, vout, capacity, p, shift, bits,
+                         static_cast<const uint32_t(*)[256]>(hist), plan.ticket_base + p, plan.tag_base + p,
+                         plan.fixed_count, desc, ctl, spin_limit, p + 1 == p1 ? plan.ranges : nullptr, plan.n_tiles,
+                         kStatusFatal | (plan.skip_on_overflow ? kStatusKeyOverflow : 0u));
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
@@ -878,7 +886,8 @@ bool launch_sort_t(KeyT* keys, uint32_t* vals, KeyT* keys_alt, uint32_t* vals_al
     uint32_t (*hist)[256] = plan.hist ? plan.hist : ctl->sort_hist;
     if (!plan.hist_ready) {
         const uint32_t hist_blocks = std::max(1u, std::min<uint32_t>(uint32_t(sms) * 4u, capacity / kHistChunk + 1u));
-        sort_histogram_kernel<<<hist_blocks, kHistThreads, 0, s>>>(keys, capacity, p0, p1, plan.key_bits, hist, ctl);
+        launch_dependent(sort_histogram_kernel<KeyT>, dim3(hist_blocks), dim3(kHistThreads), 0, s,
+                         static_cast<const KeyT*>(keys), capacity, p0, p1, plan.key_bits, hist, ctl);
     }
     if (plan.after_hist) cudaEventRecord(plan.after_hist, s);
     if constexpr (sizeof(KeyT) == 4) {  // counted passes: 32-bit keys (for 64-bit keys onesweep is faster)
