@@ -86,7 +86,12 @@ typedef struct tpd_settings {
     uint32_t key_sort_lookback;    /* 0 (default): the key sort's radix passes count every partition's digits first and
                                       scatter without waiting (counted passes, 3 CTAs per SM, or 2 with
                                       sort_ctas_per_sm = 2); 1: onesweep passes with a decoupled look-back */
-    uint32_t reserved[2];
+    uint32_t keep_backward_state;  /* whether frames keep the adjoint's inputs (per-pixel final transmittance and last
+                                      contributor; tracking them costs the blend about 5%): 0 (default) once
+                                      tpd_backward has been called on this engine; 1 always; 2 never. tpd_step_async
+                                      always keeps them; tpd_backward and a read of TPD_BUF_FINAL_T /
+                                      TPD_BUF_N_CONTRIB render the last frame again (its own views) when it kept none */
+    uint32_t reserved[1];
 } tpd_settings;
 
 /* Stages of a frame (and of a training step), for tpd_stage_times. */

@@ -41,7 +41,8 @@ class Settings(C.Structure):
         ("blend_backward_round", C.c_uint32),
         ("blend_persistent", C.c_uint32),
         ("key_sort_lookback", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("keep_backward_state", C.c_uint32),
+        ("reserved", C.c_uint32 * 1),
     ]
 
 

@@ -199,8 +199,10 @@ __device__ __forceinline__ void stage_pair_empty(PairStaged& d, uint8_t& mask) {
 // walk round r, each thread stages its entry of round r + 1 into the other
 // buffer, and one barrier per round (which also counts finished pixels)
 // separates the two. Called by the whole CTA; the first barrier comes after
-// the first staging and the last one after every read of S.
-template <uint32_t kRound>
+// the first staging and the last one after every read of S. kState: also
+// track and store each pixel's final transmittance and last contributor (the
+// adjoint's inputs); a frame that no backward follows skips that work.
+template <uint32_t kRound, bool kState>
 __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, FwdStage<kRound>& S) {
     uint32_t vi, W, H, tx, ty;
     load_view_tile(a.views, a.tile_view, tile, vi, W, H, tx, ty);
@@ -272,7 +274,6 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
                                                  skip_b ? 0.0f : fminf(kAlphaMax, ao.y));
                 const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
                 const bool term_a = tn.x < kTMin, term_b = tn.y < kTMin;  // false when skipped: tn = T
-                const bool add_a = !skip_a && !term_a, add_b = !skip_b && !term_b;
                 done_a = done_a || term_a;
                 done_b = done_b || term_b;
                 const float2 aT = __fmul2_rn(alpha, T);
@@ -281,8 +282,11 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
                 C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
                 C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
                 T = make_float2(term_a ? T.x : tn.x, term_b ? T.y : tn.y);
-                last_a = add_a ? lbase + jj : last_a;
-                last_b = add_b ? lbase + jj : last_b;
+                if constexpr (kState) {
+                    const bool add_a = !skip_a && !term_a, add_b = !skip_b && !term_b;
+                    last_a = add_a ? lbase + jj : last_a;
+                    last_b = add_b ? lbase + jj : last_b;
+                }
             }
         }
         all_done = __syncthreads_count(done_a && done_b) == kFwdThreads;
@@ -294,16 +298,20 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
             a.image[p * 3 + 0] = C0.x;
             a.image[p * 3 + 1] = C1.x;
             a.image[p * 3 + 2] = C2.x;
-            if (a.final_T) a.final_T[p] = T.x;
-            if (a.n_contrib) a.n_contrib[p] = last_a;
+            if constexpr (kState) {
+                a.final_T[p] = T.x;
+                a.n_contrib[p] = last_a;
+            }
         }
         if (in_b) {
             const size_t p = img0 + size_t(pyb) * W + px;
             a.image[p * 3 + 0] = C0.y;
             a.image[p * 3 + 1] = C1.y;
             a.image[p * 3 + 2] = C2.y;
-            if (a.final_T) a.final_T[p] = T.y;
-            if (a.n_contrib) a.n_contrib[p] = last_b;
+            if constexpr (kState) {
+                a.final_T[p] = T.y;
+                a.n_contrib[p] = last_b;
+            }
         }
     }
 }
@@ -326,7 +334,7 @@ __device__ __forceinline__ bool next_tile(FrameCtl* ctl, uint32_t slot, const ui
 
 // One CTA per tile, or (kPersistent) one CTA per resident slot taking tiles
 // from the queue.
-template <uint32_t kRound, bool kPersistent>
+template <uint32_t kRound, bool kPersistent, bool kState>
 __global__ void __launch_bounds__(kFwdThreads, fwd_min_blocks<kRound>()) blend_kernel(BlendArgs a) {
     __shared__ FwdStage<kRound> S;
     pdl_wait();  // launched as a dependent of the key sort's last pass: its lists and ranges
@@ -335,9 +343,9 @@ __global__ void __launch_bounds__(kFwdThreads, fwd_min_blocks<kRound>()) blend_k
     if (a.ctl->status & (kStatusFatal | kStatusKeyOverflow)) return;
     if constexpr (kPersistent) {
         uint32_t tile;
-        while (next_tile(a.ctl, kTicketBlend, nullptr, a.n_tiles, tile)) blend_tile<kRound>(a, tile, S);
+        while (next_tile(a.ctl, kTicketBlend, nullptr, a.n_tiles, tile)) blend_tile<kRound, kState>(a, tile, S);
     } else {
-        blend_tile<kRound>(a, blockIdx.x, S);
+        blend_tile<kRound, kState>(a, blockIdx.x, S);
     }
 }
 
@@ -645,19 +653,28 @@ int resident_ctas(Kernel k) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k, kFwdThreads, 0);
     return r > 0 ? r : 1;
 }
-template <uint32_t R, bool P>
-int blend_occupancy() { return resident_ctas(blend_kernel<R, P>); }
+template <uint32_t R, bool P, bool K>
+int blend_occupancy() { return resident_ctas(blend_kernel<R, P, K>); }
 template <uint32_t R, bool P>
 int blend_backward_occupancy() { return resident_ctas(blend_backward_kernel<R, P>); }
 
+template <uint32_t R, bool P, bool K>
+void launch_blend_k(const BlendArgs& a, int num_sms, cudaStream_t s) {
+    const uint32_t grid =
+        P ? std::min<uint32_t>(a.n_tiles, uint32_t(num_sms * device_once(blend_occupancy<R, P, K>))) : a.n_tiles;
+    if (P)  // a persistent grid is placed once: on SMs the key sort has left, not while its last CTAs run
+        blend_kernel<R, P, K><<<grid, kFwdThreads, 0, s>>>(a);
+    else
+        launch_dependent(blend_kernel<R, P, K>, dim3(grid), dim3(kFwdThreads), 0, s, a);
+}
+
+// with the adjoint's inputs (final T, last contributor) when both buffers are given
 template <uint32_t R, bool P>
 void launch_blend_t(const BlendArgs& a, int num_sms, cudaStream_t s) {
-    const uint32_t grid =
-        P ? std::min<uint32_t>(a.n_tiles, uint32_t(num_sms * device_once(blend_occupancy<R, P>))) : a.n_tiles;
-    if (P)  // a persistent grid is placed once: on SMs the key sort has left, not while its last CTAs run
-        blend_kernel<R, P><<<grid, kFwdThreads, 0, s>>>(a);
+    if (a.final_T && a.n_contrib)
+        launch_blend_k<R, P, true>(a, num_sms, s);
     else
-        launch_dependent(blend_kernel<R, P>, dim3(grid), dim3(kFwdThreads), 0, s, a);
+        launch_blend_k<R, P, false>(a, num_sms, s);
 }
 
 template <uint32_t R, bool P>

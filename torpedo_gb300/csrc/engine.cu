@@ -158,6 +158,10 @@ struct tpd_engine {
 
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
+    bool graph_state = false;      // the frame graph keeps the adjoint's inputs
+    bool body_graph_state = false; // the same for the pipelined renders' graph
+    bool state_kept = false;       // the last frame kept them (final T, last contributor)
+    bool backward_seen = false;    // tpd_backward has been called on this engine
     bool needs_eager = true;  // the first frame after any change runs without a graph
     uint64_t frames = 0;
     uint64_t tags = 0;  // frame tags issued so far (FrameCtl.tag of the last enqueued frame)
@@ -333,7 +337,8 @@ BlendLaunch blend_launch(const tpd_engine* e) {
 // Enqueues one frame on the stream (no host synchronisation).
 // io = false leaves out the uploads of the view constants and transforms and
 // the stats copy (the pipelined renders enqueue those per slot).
-void enqueue_frame(tpd_engine* e, bool io = true) {
+// state: the blend also keeps the adjoint's inputs (final T, last contributor).
+void enqueue_frame(tpd_engine* e, bool io = true, bool state = true) {
     cudaStream_t s = e->stream;
     cudaEvent_t* ev = nullptr;
     if (e->settings.stage_timing) {
@@ -449,8 +454,8 @@ void enqueue_frame(tpd_engine* e, bool io = true) {
     ba.n_tiles = e->total_tiles;
     ba.image = e->d_image;
     ba.image_offset = e->n_views > 1 ? e->d_image_offset : nullptr;
-    ba.final_T = e->d_final_T;
-    ba.n_contrib = e->d_n_contrib;
+    ba.final_T = state ? e->d_final_T : nullptr;
+    ba.n_contrib = state ? e->d_n_contrib : nullptr;
     launch_blend(ba, blend_launch(e), s);
     mark(6);
     // the backward stages of a frame without backward take no time; a
@@ -470,28 +475,54 @@ void before_frame(tpd_engine* e) {
     cudaMemsetAsync(e->d_desc_sort, 0, sort_desc_entries(uint32_t(e->capacity)) * 8, e->stream);
 }
 
+// Whether frames rendered now keep the adjoint's inputs (keep_backward_state).
+bool frame_state(const tpd_engine* e) {
+    return e->settings.keep_backward_state == 1 || (e->settings.keep_backward_state == 0 && e->backward_seen);
+}
+
+// The frame graph, captured again when it was captured with the other state choice.
+int ensure_frame_graph(tpd_engine* e, bool state) {
+    if (e->graph_valid && e->graph_state == state) return TPD_OK;
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+    e->graph_valid = false;
+    cudaGraph_t g = nullptr;
+    TPD_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_frame(e, true, state);
+    TPD_CUDA(e, cudaStreamEndCapture(e->stream, &g));
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    TPD_CUDA(e, err);
+    e->graph = ge;
+    e->graph_valid = true;
+    e->graph_state = state;
+    return TPD_OK;
+}
+
 int run_frame_once(tpd_engine* e, bool use_graph) {
+    const bool state = frame_state(e);
     if (use_graph) {
-        if (!e->graph_valid) {
-            cudaGraph_t g = nullptr;
-            TPD_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_frame(e);
-            TPD_CUDA(e, cudaStreamEndCapture(e->stream, &g));
-            cudaGraphExec_t ge = nullptr;
-            const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
-            cudaGraphDestroy(g);
-            TPD_CUDA(e, err);
-            e->graph = ge;
-            e->graph_valid = true;
-        }
+        const int rc = ensure_frame_graph(e, state);
+        if (rc != TPD_OK) return rc;
         before_frame(e);
         TPD_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
     } else {
         before_frame(e);
-        enqueue_frame(e);
+        enqueue_frame(e, true, state);
         TPD_CUDA(e, cudaGetLastError());
     }
+    e->state_kept = state;
     return wait_stream(e);
+}
+
+// Renders the last frame again, keeping the adjoint's inputs: from the device
+// copies of its view constants and transforms, so a camera set since then
+// does not enter. Enqueued only.
+void rerender_with_state(tpd_engine* e) {
+    before_frame(e);
+    enqueue_frame(e, false, true);
+    e->state_kept = true;
 }
 
 int set_views_internal(tpd_engine* e, const tpd_view* views, uint32_t nv) {
@@ -883,24 +914,18 @@ int tpd_raster_frames_async(tpd_engine* e, uint32_t count) {
         return fail(e, TPD_ERR_STATE, "render one frame with tpd_raster_frame after any change first");
     cudaSetDevice(e->device);
     const bool graph = e->settings.use_graph && !e->settings.stage_timing;
-    if (graph && !e->graph_valid) {
-        cudaGraph_t g = nullptr;
-        TPD_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_frame(e);
-        TPD_CUDA(e, cudaStreamEndCapture(e->stream, &g));
-        cudaGraphExec_t ge = nullptr;
-        const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
-        cudaGraphDestroy(g);
-        TPD_CUDA(e, err);
-        e->graph = ge;
-        e->graph_valid = true;
+    const bool state = frame_state(e);
+    if (graph) {
+        const int rc = ensure_frame_graph(e, state);
+        if (rc != TPD_OK) return rc;
     }
     for (uint32_t i = 0; i < count; ++i) {
         before_frame(e);
         if (graph) TPD_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
-        else enqueue_frame(e);
+        else enqueue_frame(e, true, state);
     }
     TPD_CUDA(e, cudaGetLastError());
+    if (count) e->state_kept = state;
     e->frames += count;
     return TPD_OK;
 }
@@ -947,24 +972,31 @@ int tpd_render_async(tpd_engine* e, void* dst, uint32_t format, int dst_is_devic
                                     cudaMemcpyHostToDevice, s));
     }
     const bool graph = e->settings.use_graph && !e->settings.stage_timing;
+    const bool state = frame_state(e);
     if (graph) {
+        if (e->body_graph && e->body_graph_state != state) {
+            cudaGraphExecDestroy(e->body_graph);
+            e->body_graph = nullptr;
+        }
         if (!e->body_graph) {
             cudaGraph_t g = nullptr;
             TPD_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            enqueue_frame(e, false);
+            enqueue_frame(e, false, state);
             TPD_CUDA(e, cudaStreamEndCapture(s, &g));
             cudaGraphExec_t ge = nullptr;
             const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
             cudaGraphDestroy(g);
             TPD_CUDA(e, err);
             e->body_graph = ge;
+            e->body_graph_state = state;
         }
         before_frame(e);
         TPD_CUDA(e, cudaGraphLaunch(e->body_graph, s));
     } else {
         before_frame(e);
-        enqueue_frame(e, false);
+        enqueue_frame(e, false, state);
     }
+    e->state_kept = state;
     // image into the slot's staging buffer and stats into its pinned slot
     uint64_t bytes;
     if (format == TPD_IMAGE_RGBA8) {
@@ -1129,9 +1161,11 @@ int tpd_backward(tpd_engine* e, const float* dL_dimage, float* g_means, float* g
     if (!e || !dL_dimage) return TPD_ERR_ARG;
     if (!e->frame_valid) return fail(e, TPD_ERR_STATE, "backward before a rendered frame");
     cudaSetDevice(e->device);
+    e->backward_seen = true;  // with keep_backward_state 0, later frames keep the adjoint's inputs
     BackwardOut o{g_means, g_log_scales, g_quats, g_logits, g_sh};
     const int rc = prepare_backward(e, o);
     if (rc != TPD_OK) return rc;
+    if (!e->state_kept) rerender_with_state(e);
     enqueue_backward(e, dL_dimage, o);
     TPD_CUDA(e, cudaGetLastError());
     return wait_stream(e);
@@ -1172,6 +1206,7 @@ int tpd_step_async(tpd_engine* e, const float* dL_dimage, float* g_means, float*
         }
     }
     TPD_CUDA(e, cudaGetLastError());
+    if (count) e->state_kept = true;  // a training step's frame keeps the adjoint's inputs
     e->frames += count;
     return TPD_OK;
 }
@@ -1203,6 +1238,14 @@ int tpd_get_buffer(const tpd_engine* e, uint32_t which, void** ptr, uint64_t* by
     if (!e || !ptr) return TPD_ERR_ARG;
     if (which == TPD_BUF_KEYS && e->capacity > 0) {
         const int rc = rebuild_keys(const_cast<tpd_engine*>(e));  // a read-back cache, not engine state
+        if (rc != TPD_OK) return rc;
+    }
+    if ((which == TPD_BUF_FINAL_T || which == TPD_BUF_N_CONTRIB) && e->frame_valid && !e->state_kept) {
+        tpd_engine* m = const_cast<tpd_engine*>(e);  // the same frame, with the buffers asked for
+        cudaSetDevice(m->device);
+        rerender_with_state(m);
+        TPD_CUDA(m, cudaGetLastError());
+        const int rc = wait_stream(m);
         if (rc != TPD_OK) return rc;
     }
     const int b = e->sorted_in_alt ? 1 : 0;

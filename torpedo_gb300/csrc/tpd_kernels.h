@@ -170,8 +170,10 @@ struct BlendArgs {
     uint32_t n_tiles;
     float* image;             // HWC float3 per view, packed per view at image_offset[view]
     const uint64_t* image_offset;  // per view pixel offset (nullptr: 0)
-    float* final_T;           // per pixel (nullable)
-    uint32_t* n_contrib;      // per pixel (nullable)
+    // per pixel: final transmittance and list entries up to the last
+    // contributor (the adjoint's inputs); both null: not tracked
+    float* final_T;
+    uint32_t* n_contrib;
 };
 // Launch settings of the blend and its adjoint: list entries per staged
 // round (forward 64 / 128 / 256, adjoint 32 / 64 / 128) and the form of the

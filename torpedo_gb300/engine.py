@@ -151,7 +151,8 @@ class GaussianEngine:
                  use_graph: bool = True, spin_limit: int = 0, initial_key_capacity: int = 0, timeout_s: float = 60.0,
                  test_never_publish: bool = False, stage_timing: bool = False, sort_ctas_per_sm: int = 0,
                  depth_sort_items: int = 0, sort_threads: int = 0, depth_sort_threads: int = 0, blend_round: int = 0,
-                 blend_backward_round: int = 0, blend_persistent: bool = False, key_sort_lookback: bool = False):
+                 blend_backward_round: int = 0, blend_persistent: bool = False, key_sort_lookback: bool = False,
+                 keep_backward_state: int = 0):
         lib = L.load()
         s = L.Settings()
         lib.tpd_settings_init(C.byref(s))
@@ -173,6 +174,7 @@ class GaussianEngine:
         s.blend_backward_round = blend_backward_round
         s.blend_persistent = 1 if blend_persistent else 0
         s.key_sort_lookback = 1 if key_sort_lookback else 0
+        s.keep_backward_state = keep_backward_state
         h = C.c_void_p()
         _check(lib.tpd_create(C.byref(s), C.byref(h)))
         self._h = h
