@@ -412,13 +412,15 @@ void enqueue_frame(tpd_engine* e, bool io = true, bool state = true) {
     dp.compact_culled = true;  // culled items leave in the first pass; the rest sort ctl->depth_count
     e->depth_in_alt = launch_sort(e->d_dkeys[0], e->d_ditems[0], e->d_dkeys[1], e->d_ditems[1], items, dp,
                                   e->d_desc_depth, e->d_ctl, spin, e->num_sms, s);
+    // the order is in the other buffer when a pass skipped (ctl->depth_skips odd)
     const uint32_t* order = e->d_ditems[e->depth_in_alt ? 1 : 0];
-    launch_depth_scan(e->d_splats, order, items, e->d_offsets, e->d_desc_pre, e->d_ctl, spin,
+    const uint32_t* order_other = e->d_ditems[e->depth_in_alt ? 0 : 1];
+    launch_depth_scan(e->d_splats, order, order_other, items, e->d_offsets, e->d_desc_pre, e->d_ctl, spin,
                       e->settings.test_never_publish, s);
     mark(2);
     const uint32_t cap = uint32_t(e->capacity);
-    launch_keygen(e->d_splats, order, e->d_offsets, items, e->n, e->d_views, e->d_tiles[0], e->d_vals[0], cap,
-                  e->key_bits, e->d_ranges, e->total_tiles, e->d_ctl, e->num_sms, s);
+    launch_keygen(e->d_splats, order, order_other, e->d_offsets, items, e->n, e->d_views, e->d_tiles[0], e->d_vals[0],
+                  cap, e->key_bits, e->d_ranges, e->total_tiles, e->d_ctl, e->num_sms, s);
     mark(3);
     SortPlan kp;
     kp.first_bit = 0;  // tile ids; the depth half of the keys is already in order

@@ -53,7 +53,8 @@ struct KeygenSmem {
 
 __global__ void __launch_bounds__(kKeygenThreads)
     keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
-                  const uint32_t* __restrict__ offsets, uint32_t n_items, uint32_t n,
+                  const uint32_t* __restrict__ items_other, const uint32_t* __restrict__ offsets, uint32_t n_items,
+                  uint32_t n,
                   const ViewConst* __restrict__ views, uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals,
                   uint32_t capacity, uint32_t key_bits, uint32_t* __restrict__ ranges, uint32_t n_tiles,
                   FrameCtl* ctl) {
@@ -66,6 +67,7 @@ __global__ void __launch_bounds__(kKeygenThreads)
     if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
     if (ctl->status & kStatusFatal) return;
     const uint32_t count = min(ctl->depth_count, n_items);
+    if (ctl->depth_skips & 1u) items = items_other;  // a skipped depth pass left the order there
     // ranges: (0xFFFFFFFF, 0) until the key sort's last pass narrows them
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x)
         reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0xFFFFFFFFu, 0u);
@@ -197,7 +199,8 @@ int keygen_setup() {
 
 }  // namespace
 
-void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
+void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* items_other, const uint32_t* offsets,
+                   uint32_t n_items, uint32_t n,
                    const ViewConst* views, uint32_t* tiles, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
                    uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s) {
     if (n_items == 0 || n == 0) return;
@@ -206,8 +209,8 @@ void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* o
     const int per_sm = device_once(keygen_setup);  // resident CTAs per SM (shared memory bound)
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
     blocks = blocks < cap ? blocks : cap;
-    launch_dependent(keygen_kernel, dim3(unsigned(blocks)), dim3(kKeygenThreads), 0, s, splats, items, offsets,
-                     n_items, n, views, tiles, vals, capacity, key_bits, ranges, n_tiles, ctl);
+    launch_dependent(keygen_kernel, dim3(unsigned(blocks)), dim3(kKeygenThreads), 0, s, splats, items, items_other,
+                     offsets, n_items, n, views, tiles, vals, capacity, key_bits, ranges, n_tiles, ctl);
 }
 
 namespace {

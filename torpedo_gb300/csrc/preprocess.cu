@@ -84,6 +84,7 @@ __global__ void frame_begin_kernel(FrameCtl* ctl, const float* transforms, uint3
         ctl->total_keys = 0;
         ctl->visible = 0;
         ctl->depth_count = 0;
+        ctl->depth_skips = 0;
     }
     if (!views || !ent_mats) return;
     for (uint32_t ve = t; ve < n_views * n_ent; ve += blockDim.x) {
@@ -450,8 +451,8 @@ constexpr uint32_t kScanThreads = 256;
 // (at most n): the grid is sized for n and the partitions past the count exit.
 template <bool kGather, uint32_t kItems>
 __global__ void __launch_bounds__(kScanThreads)
-    scan_tiles_kernel(const Splat* splats, const uint32_t* items, uint32_t n_max, uint32_t* offsets, uint64_t* desc,
-                      FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish) {
+    scan_tiles_kernel(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t n_max,
+                      uint32_t* offsets, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish) {
     constexpr uint32_t kScanTile = kScanThreads * kItems;
     __shared__ uint32_t s_part, s_excl;
     // launched as a dependent of the stream's previous kernel: its output is
@@ -461,6 +462,7 @@ __global__ void __launch_bounds__(kScanThreads)
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t n = kGather ? min(ctl->depth_count, n_max) : n_max;
+    if (kGather && (ctl->depth_skips & 1u)) items = items_other;  // a skipped depth pass left the order there
     if (tid == 0) s_part = atomicAdd(&ctl->ticket[kTicketScan], 1u);
     __syncthreads();
     const uint32_t part = s_part;
@@ -569,16 +571,17 @@ void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint6
                        uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
     if (n == 0) return;
     const uint32_t blocks = (n + kScanThreads * 4 - 1) / (kScanThreads * 4);
-    scan_tiles_kernel<false, 4><<<blocks, kScanThreads, 0, s>>>(splats, nullptr, n, offsets, desc, ctl, spin_limit,
-                                                                never_publish);
+    scan_tiles_kernel<false, 4><<<blocks, kScanThreads, 0, s>>>(splats, nullptr, nullptr, n, offsets, desc, ctl,
+                                                                spin_limit, never_publish);
 }
 
-void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t max_count, uint32_t* offsets,
-                       uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
+void launch_depth_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t max_count,
+                       uint32_t* offsets, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish,
+                       cudaStream_t s) {
     if (max_count == 0) return;
     const uint32_t blocks = (max_count + kScanThreads * 16 - 1) / (kScanThreads * 16);
-    launch_dependent(scan_tiles_kernel<true, 16>, dim3(blocks), dim3(kScanThreads), 0, s, splats, items, max_count,
-                     offsets, desc, ctl, spin_limit, never_publish);
+    launch_dependent(scan_tiles_kernel<true, 16>, dim3(blocks), dim3(kScanThreads), 0, s, splats, items, items_other,
+                     max_count, offsets, desc, ctl, spin_limit, never_publish);
 }
 
 void launch_pack_records(const float* means, const float* log_scales, const float* quats, const float* logits,

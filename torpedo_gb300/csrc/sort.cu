@@ -50,7 +50,7 @@ constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K (and 
 // the others, where a pass whose digit is the same for every key is a copy.
 constexpr int kPassPlain = 0;      // K = fixed_count, else ctl->total_keys
 constexpr int kPassDropCulled = 1; // as plain; keys whose low 32 bits are 0xFFFFFFFF are not written
-constexpr int kPassCompacted = 2;  // K = ctl->depth_count; a uniform digit makes the pass a copy
+constexpr int kPassCompacted = 2;  // K = ctl->depth_count; a uniform digit skips the pass (ctl->depth_skips)
 
 constexpr uint32_t kHistThreads = 256;
 constexpr uint32_t kHistChunk = 2048;  // keys per grid-stride chunk of the histogram kernel
@@ -196,34 +196,6 @@ __device__ __forceinline__ uint32_t digit_lookback(const uint64_t* __restrict__ 
     return excl;
 }
 
-// keys_out / vals_out [0, K) = keys_in / vals_in: thread t of nthr moves
-// 16-byte vectors (16 / sizeof(KeyT) keys, four values), kUnroll loads in
-// flight before their stores; scalar when a buffer is not 16-byte aligned.
-template <uint32_t kUnroll, typename KeyT>
-__device__ __forceinline__ void copy_pairs(const KeyT* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-                                           KeyT* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t K,
-                                           uint32_t t, uint32_t nthr) {
-    constexpr uint32_t kPerVec = 16 / sizeof(KeyT);
-    const bool vec = ((reinterpret_cast<uintptr_t>(keys_in) | reinterpret_cast<uintptr_t>(keys_out) |
-                       reinterpret_cast<uintptr_t>(vals_in) | reinterpret_cast<uintptr_t>(vals_out)) & 15u) == 0;
-    const uint32_t nk = vec ? K / kPerVec : 0u, nv = vec ? K / 4 : 0u;
-    auto copy16 = [&](const uint4* __restrict__ src, uint4* __restrict__ dst, uint32_t n) {
-        for (uint32_t i0 = t; i0 < n; i0 += nthr * kUnroll) {
-            uint4 r[kUnroll];
-#pragma unroll
-            for (uint32_t u = 0; u < kUnroll; ++u)
-                if (i0 + u * nthr < n) r[u] = src[i0 + u * nthr];
-#pragma unroll
-            for (uint32_t u = 0; u < kUnroll; ++u)
-                if (i0 + u * nthr < n) dst[i0 + u * nthr] = r[u];
-        }
-    };
-    copy16(reinterpret_cast<const uint4*>(keys_in), reinterpret_cast<uint4*>(keys_out), nk);
-    copy16(reinterpret_cast<const uint4*>(vals_in), reinterpret_cast<uint4*>(vals_out), nv);
-    for (uint32_t i = kPerVec * nk + t; i < K; i += nthr) keys_out[i] = keys_in[i];
-    for (uint32_t i = 4 * nv + t; i < K; i += nthr) vals_out[i] = vals_in[i];
-}
-
 // Tile ranges (range.slang:18-35) from the last pass of the key sort: the
 // partition's keys sit in shared memory fully sorted within each digit run,
 // and a digit run is contiguous in the output. A tile starts where the run's
@@ -286,6 +258,16 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                            : min(kPass == kPassCompacted ? ctl->depth_count
                                                          : (fixed_count ? fixed_count : ctl->total_keys),
                                  capacity);
+    if constexpr (kPass == kPassCompacted) {
+        if (ctl->depth_skips & 1u) {  // an earlier pass was skipped: its input buffer holds the order
+            KeyT* const k = const_cast<KeyT*>(keys_in);
+            keys_in = keys_out;
+            keys_out = k;
+            uint32_t* const v = const_cast<uint32_t*>(vals_in);
+            vals_in = vals_out;
+            vals_out = v;
+        }
+    }
     const uint32_t nparts = (K + kSortTile - 1) / kSortTile;
     const uint32_t tag = ctl->tag * 32u + tag_slot;
     const uint32_t mask = (1u << bits) - 1u;
@@ -301,10 +283,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     }
     if constexpr (kPass == kPassCompacted) {
         // a pass whose digit is the same for all K keys leaves their order as
-        // it is: the grid copies them
+        // it is: it is skipped and counted, and the order stays in its input
+        // buffer (every CTA takes the same decision from the same histogram)
         if (__syncthreads_or(digit_thread && K > 0 && h == K)) {
-            copy_pairs<kItems >= 16 ? 8u : 4u>(keys_in, vals_in, keys_out, vals_out, K, blockIdx.x * kThreads + tid,
-                                               gridDim.x * kThreads);
+            if (blockIdx.x == 0 && tid == 0) atomicAdd(&ctl->depth_skips, 1u);
             return;
         }
     }

@@ -22,7 +22,11 @@ struct FrameCtl {
     uint32_t depth_hist[8][256];  // digit counts of the depth sort, by 8-bit digit position
     uint32_t debug[4];       // site, index, bound of the first failed index guard
     uint32_t depth_count;    // (view, Gaussian) items with a non-empty tile rect: those the depth sort keeps
-    uint32_t pad[3];
+    // depth-sort passes skipped because their digit was the same for every
+    // key (the order stays in the pass's input buffer): when odd, the later
+    // passes swap their buffers and the sorted items are in the other one
+    uint32_t depth_skips;
+    uint32_t pad[2];
 };
 
 // Entity matrices: rows 0..2 of view*model and rows 0..3 of projview*model.
@@ -82,8 +86,11 @@ void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s);
 // (at most max_count), gathered through items[r] = v * n + i, scanned into
 // exclusive key offsets offsets[r]; the total goes to ctl->total_keys and the
 // non-empty count to ctl->visible.
-void launch_depth_scan(const Splat* splats, const uint32_t* items, uint32_t max_count, uint32_t* offsets,
-                       uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, cudaStream_t s);
+// items: where the depth sort leaves the order with no pass skipped;
+// items_other: the other buffer, which holds it when ctl->depth_skips is odd.
+void launch_depth_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t max_count,
+                       uint32_t* offsets, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish,
+                       cudaStream_t s);
 
 // Standalone exclusive scan of Splat.tiles (prefix.slang); total -> ctl->total_keys.
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
@@ -98,9 +105,10 @@ void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint6
 // ranges (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
 // The digit counts of the tile ids come from the preprocess (tile_bits).
 // items[0 .. ctl->depth_count) index the n_items = n_views x n splats.
-void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* offsets, uint32_t n_items, uint32_t n,
-                   const ViewConst* views, uint32_t* tiles, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
-                   uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s);
+void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* items_other, const uint32_t* offsets,
+                   uint32_t n_items, uint32_t n, const ViewConst* views, uint32_t* tiles, uint32_t* vals,
+                   uint32_t capacity, uint32_t key_bits, uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl,
+                   int num_sms, cudaStream_t s);
 
 // keys[i] = tiles[i] << 32 | bits(viewZ of splat vals[i] in the tile's view),
 // i < min(ctl->total_keys, capacity): the 64-bit (tile | depth) keys of a
