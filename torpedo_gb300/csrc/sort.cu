@@ -521,9 +521,6 @@ __global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __rest
     const uint32_t part = blockIdx.x;
     if (part >= nparts) return;  // (uniform)
     const uint32_t mask = (1u << bits) - 1u;
-#pragma unroll
-    for (uint32_t w = 0; w < 8; ++w) hw[w][tid] = 0;
-    __syncthreads();
     const uint32_t base = part * kTile, cnt = min(kTile, K - base);
     KeyT k[kItems];
 #pragma unroll
@@ -531,6 +528,10 @@ __global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __rest
         const uint32_t idx = i * 256 + tid;
         k[i] = idx < cnt ? keys[base + idx] : KeyT(0);
     }
+    // (while the loads are in flight) each warp clears its own counts
+#pragma unroll
+    for (uint32_t j = 0; j < kRadix / 32; ++j) hw[warp][lane + 32 * j] = 0;
+    __syncwarp();
     // 32 consecutive keys often share a digit (a Gaussian's row of tiles, in
     // the high digit): then one add of 32, else one shared atomic per key
 #pragma unroll
