@@ -235,12 +235,18 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
         }
     };
 
+    // Without the adjoint's inputs a pixel that stops is frozen at T = 0: every
+    // later pair then adds exactly nothing, so no per-pixel done flags are
+    // needed (pixels outside the image start frozen). With them, T must stay
+    // the transmittance at the stop, and done flags gate the later pairs.
     bool done_a = !in_a, done_b = !in_b;
-    float2 T = make_float2(1.0f, 1.0f), C0 = make_float2(0.f, 0.f), C1 = C0, C2 = C0;
+    float2 T = make_float2(kState || in_a ? 1.0f : 0.0f, kState || in_b ? 1.0f : 0.0f);
+    float2 C0 = make_float2(0.f, 0.f), C1 = C0, C2 = C0;
     uint32_t last_a = 0, last_b = 0;
     const float2 one = make_float2(1.0f, 1.0f), mone = make_float2(-1.0f, -1.0f);
+    auto pixels_done = [&]() { return kState ? done_a && done_b : T.x == 0.0f && T.y == 0.0f; };
     if (start < end) stage(0, start);
-    bool all_done = __syncthreads_count(done_a && done_b) == kFwdThreads;
+    bool all_done = __syncthreads_count(pixels_done()) == kFwdThreads;
     uint32_t r = 0;
     for (uint32_t b0 = start; b0 < end && !all_done; b0 += kRound, ++r) {
         const uint32_t b = r & 1u;
@@ -249,7 +255,7 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
         const uint32_t n = min(kRound, end - b0);
         const uint32_t lbase = b0 - start + 1u;  // n_contrib of entry jj of this round: lbase + jj
         for (uint32_t g = 0; g < n; g += 32) {
-            if (__all_sync(0xFFFFFFFFu, done_a && done_b)) break;
+            if (__all_sync(0xFFFFFFFFu, pixels_done())) break;
             const uint32_t e = g + lane;
             uint32_t m = __ballot_sync(0xFFFFFFFFu, e < n && ((S.mask[b][e] >> warp) & 1u));
             // branch-free body: every lane evaluates both pairs and selects
@@ -268,28 +274,41 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
                 const float2 p2 = __ffma2_rn(t, dx, __fmul2_rn(__fmul2_rn(make_float2(qco.x, qco.y), dy), dy));
                 const float2 ao =
                     __fmul2_rn(make_float2(qco.z, qco.w), make_float2(ex2_approx(p2.x), ex2_approx(p2.y)));
-                const bool skip_a = done_a || pair_skipped(p2.x, bt.z);
-                const bool skip_b = done_b || pair_skipped(p2.y, bt.z);
-                const float2 alpha = make_float2(skip_a ? 0.0f : fminf(kAlphaMax, ao.x),
-                                                 skip_b ? 0.0f : fminf(kAlphaMax, ao.y));
-                const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
-                const bool term_a = tn.x < kTMin, term_b = tn.y < kTMin;  // false when skipped: tn = T
-                done_a = done_a || term_a;
-                done_b = done_b || term_b;
-                const float2 aT = __fmul2_rn(alpha, T);
-                const float2 w = make_float2(term_a ? 0.0f : aT.x, term_b ? 0.0f : aT.y);
-                C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
-                C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
-                C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
-                T = make_float2(term_a ? T.x : tn.x, term_b ? T.y : tn.y);
                 if constexpr (kState) {
+                    const bool skip_a = done_a || pair_skipped(p2.x, bt.z);
+                    const bool skip_b = done_b || pair_skipped(p2.y, bt.z);
+                    const float2 alpha = make_float2(skip_a ? 0.0f : fminf(kAlphaMax, ao.x),
+                                                     skip_b ? 0.0f : fminf(kAlphaMax, ao.y));
+                    const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
+                    const bool term_a = tn.x < kTMin, term_b = tn.y < kTMin;  // false when skipped: tn = T
+                    done_a = done_a || term_a;
+                    done_b = done_b || term_b;
+                    const float2 aT = __fmul2_rn(alpha, T);
+                    const float2 w = make_float2(term_a ? 0.0f : aT.x, term_b ? 0.0f : aT.y);
+                    C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
+                    C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
+                    C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
+                    T = make_float2(term_a ? T.x : tn.x, term_b ? T.y : tn.y);
                     const bool add_a = !skip_a && !term_a, add_b = !skip_b && !term_b;
                     last_a = add_a ? lbase + jj : last_a;
                     last_b = add_b ? lbase + jj : last_b;
+                } else {
+                    // keep = 0 at the stop and after it (T = 0 gives tn = 0):
+                    // the pair adds alpha T * 0 = 0 and T becomes 0; before
+                    // the stop keep = 1 and both products are exact copies
+                    const float2 alpha = make_float2(pair_skipped(p2.x, bt.z) ? 0.0f : fminf(kAlphaMax, ao.x),
+                                                     pair_skipped(p2.y, bt.z) ? 0.0f : fminf(kAlphaMax, ao.y));
+                    const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
+                    const float2 keep = make_float2(tn.x < kTMin ? 0.0f : 1.0f, tn.y < kTMin ? 0.0f : 1.0f);
+                    const float2 w = __fmul2_rn(__fmul2_rn(alpha, T), keep);
+                    C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
+                    C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
+                    C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
+                    T = __fmul2_rn(tn, keep);
                 }
             }
         }
-        all_done = __syncthreads_count(done_a && done_b) == kFwdThreads;
+        all_done = __syncthreads_count(pixels_done()) == kFwdThreads;
     }
     if (TPD_INBOUNDS(a.ctl, 41, tile, a.n_tiles)) {
         const size_t img0 = a.image_offset ? a.image_offset[vi] : 0ull;
