@@ -243,12 +243,14 @@ def general_sort(eng, K, key_bits, stream, steps):
             "input": "the frame's keys in a seeded random order; timed with CUDA events, median"}
 
 
-def kernels_per_frame(views: int, tile_passes: int) -> int:
-    """Kernel launches of one frame: frame_begin, preprocess, depth-sort passes,
-    depth-order scan, keygen, tile-id sort passes (the last one also writes the
-    tile ranges), blend."""
+def kernels_per_frame(views: int, tile_passes: int, counted: bool = True) -> int:
+    """Kernel launches of one frame: frame_begin, preprocess, depth-sort passes
+    (a pass whose digit is the same for every key launches and returns),
+    depth-order scan, keygen, tile-id sort passes (counted passes: a counting
+    and a scatter kernel each; the last scatter also writes the tile ranges),
+    blend."""
     depth_passes = math.ceil((32 + (views - 1).bit_length()) / 8)
-    return 5 + depth_passes + tile_passes
+    return 5 + depth_passes + tile_passes * (2 if counted else 1)
 
 
 def _params(sc, dev):
@@ -446,7 +448,9 @@ def run_ours(args):
         e.raster_frame()
         return e
 
-    if args.sort_ctas:
+    if args.no_autotune:
+        settings, tuned = {}, None  # the engine's defaults
+    elif args.sort_ctas:
         settings, tuned = {"sort_ctas_per_sm": args.sort_ctas, "sort_threads": args.sort_threads,
                            "depth_sort_items": args.depth_sort_items,
                            "depth_sort_threads": args.depth_sort_threads}, None
@@ -456,7 +460,7 @@ def run_ours(args):
         settings, tuned = autotune.tune(make_engine, lambda e, k: e.raster_frames_async(k), stream)
     eng = make_engine(settings)
     st = eng.raster_frame()
-    launches_per_frame = kernels_per_frame(1, int(st["sort_passes"]))
+    launches_per_frame = kernels_per_frame(1, int(st["sort_passes"]), not settings.get("key_sort_lookback", 0))
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -665,6 +669,7 @@ def main():
     ap.add_argument("--sort-threads", type=int, default=0, help="with --sort-ctas: radix CTA size (256 or 512)")
     ap.add_argument("--depth-sort-items", type=int, default=0, help="with --sort-ctas: depth sort keys per thread")
     ap.add_argument("--depth-sort-threads", type=int, default=0, help="with --sort-ctas: depth sort CTA size (256 or 512)")
+    ap.add_argument("--no-autotune", action="store_true", help="the engine's default settings (e.g. for a profiler)")
     ap.add_argument("--no-train", action="store_true", help="skip the cfg2, cfg3 and cfg4 forward+backward measurements")
     ap.add_argument("--no-large", action="store_true", help="skip the cfg4 forward+backward measurement")
     ap.add_argument("--train-only", action="store_true", help="only the cfg2 forward+backward steps (profiling)")
