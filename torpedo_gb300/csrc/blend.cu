@@ -235,16 +235,16 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
         }
     };
 
-    // Without the adjoint's inputs a pixel that stops is frozen at T = 0: every
-    // later pair then adds exactly nothing, so no per-pixel done flags are
-    // needed (pixels outside the image start frozen). With them, T must stay
-    // the transmittance at the stop, and done flags gate the later pairs.
-    bool done_a = !in_a, done_b = !in_b;
-    float2 T = make_float2(kState || in_a ? 1.0f : 0.0f, kState || in_b ? 1.0f : 0.0f);
+    // A pixel that stops is frozen at T = 0: every later pair then adds
+    // exactly nothing, so no per-pixel done flags are needed (pixels outside
+    // the image start frozen). With the adjoint's inputs, Tk keeps the
+    // transmittance at the stop, which is what the reference leaves.
+    float2 T = make_float2(in_a ? 1.0f : 0.0f, in_b ? 1.0f : 0.0f);
+    float2 Tk = make_float2(1.0f, 1.0f);  // kState: the transmittance to store (it stays at the stop)
     float2 C0 = make_float2(0.f, 0.f), C1 = C0, C2 = C0;
     uint32_t last_a = 0, last_b = 0;
     const float2 one = make_float2(1.0f, 1.0f), mone = make_float2(-1.0f, -1.0f);
-    auto pixels_done = [&]() { return kState ? done_a && done_b : T.x == 0.0f && T.y == 0.0f; };
+    auto pixels_done = [&]() { return T.x == 0.0f && T.y == 0.0f; };
     if (start < end) stage(0, start);
     bool all_done = __syncthreads_count(pixels_done()) == kFwdThreads;
     uint32_t r = 0;
@@ -275,23 +275,23 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
                 const float2 ao =
                     __fmul2_rn(make_float2(qco.z, qco.w), make_float2(ex2_approx(p2.x), ex2_approx(p2.y)));
                 if constexpr (kState) {
-                    const bool skip_a = done_a || pair_skipped(p2.x, bt.z);
-                    const bool skip_b = done_b || pair_skipped(p2.y, bt.z);
-                    const float2 alpha = make_float2(skip_a ? 0.0f : fminf(kAlphaMax, ao.x),
-                                                     skip_b ? 0.0f : fminf(kAlphaMax, ao.y));
+                    // the frozen form below, plus Tk, the transmittance as the
+                    // reference keeps it (it stays at the stop), and the last
+                    // entry that added: w > 0 exactly when the pair adds
+                    // (alpha >= 1/255 times T >= 1e-4)
+                    const float2 alpha = make_float2(pair_skipped(p2.x, bt.z) ? 0.0f : fminf(kAlphaMax, ao.x),
+                                                     pair_skipped(p2.y, bt.z) ? 0.0f : fminf(kAlphaMax, ao.y));
                     const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
-                    const bool term_a = tn.x < kTMin, term_b = tn.y < kTMin;  // false when skipped: tn = T
-                    done_a = done_a || term_a;
-                    done_b = done_b || term_b;
-                    const float2 aT = __fmul2_rn(alpha, T);
-                    const float2 w = make_float2(term_a ? 0.0f : aT.x, term_b ? 0.0f : aT.y);
+                    const bool go_a = !(tn.x < kTMin), go_b = !(tn.y < kTMin);
+                    const float2 keep = make_float2(go_a ? 1.0f : 0.0f, go_b ? 1.0f : 0.0f);
+                    const float2 w = __fmul2_rn(__fmul2_rn(alpha, T), keep);
                     C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
                     C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
                     C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
-                    T = make_float2(term_a ? T.x : tn.x, term_b ? T.y : tn.y);
-                    const bool add_a = !skip_a && !term_a, add_b = !skip_b && !term_b;
-                    last_a = add_a ? lbase + jj : last_a;
-                    last_b = add_b ? lbase + jj : last_b;
+                    T = __fmul2_rn(tn, keep);
+                    Tk = make_float2(go_a ? tn.x : Tk.x, go_b ? tn.y : Tk.y);
+                    last_a = w.x > 0.0f ? lbase + jj : last_a;
+                    last_b = w.y > 0.0f ? lbase + jj : last_b;
                 } else {
                     // keep = 0 at the stop and after it (T = 0 gives tn = 0):
                     // the pair adds alpha T * 0 = 0 and T becomes 0; before
@@ -318,7 +318,7 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
             a.image[p * 3 + 1] = C1.x;
             a.image[p * 3 + 2] = C2.x;
             if constexpr (kState) {
-                a.final_T[p] = T.x;
+                a.final_T[p] = Tk.x;
                 a.n_contrib[p] = last_a;
             }
         }
@@ -328,7 +328,7 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
             a.image[p * 3 + 1] = C1.y;
             a.image[p * 3 + 2] = C2.y;
             if constexpr (kState) {
-                a.final_T[p] = T.y;
+                a.final_T[p] = Tk.y;
                 a.n_contrib[p] = last_b;
             }
         }

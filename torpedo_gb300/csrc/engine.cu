@@ -1314,10 +1314,13 @@ int tpd_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t*
     plan.key_bits = key_bits;
     plan.hist = ctl->sort_hist;
     plan.hist_ready = false;
-    // 512 threads x 8 keys per 4096-key partition with a look-back: on 64-bit
-    // keys faster than the counted passes (0.85 against 1.06 ms for 9M keys
-    // of 45 bits), which serve the frame's 32-bit key sort
-    plan.threads = 512;
+    // onesweep passes of 256 threads x 16 keys (ballot ranking, 2 CTAs per SM)
+    // with a look-back: on 64-bit keys faster than 512 x 8 keys with match
+    // ranking (0.845 against 0.910 ms for 9M random keys of 45 bits, the
+    // histogram kernel included) and than the counted passes that serve the
+    // frame's 32-bit key sort
+    plan.threads = 256;
+    plan.ctas_per_sm = 2;
     const bool alt = launch_sort(keys, vals, keys_alt, vals_alt, n, plan, desc, ctl, kDefaultSpin, sms, s);
     *result_in_alt = alt ? 1 : 0;
     return cudaGetLastError() == cudaSuccess ? TPD_OK : TPD_ERR_DEVICE;
