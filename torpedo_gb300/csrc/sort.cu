@@ -27,6 +27,7 @@
 // The result is the stable sort of the pairs by the low key_bits bits, the
 // same permutation as the reference's sort.
 #include <algorithm>
+#include <type_traits>
 
 #include "tpd_common.cuh"
 #include "tpd_kernels.h"
@@ -626,95 +627,116 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     if (part >= nparts) return;  // (uniform)
     const uint32_t mask = (1u << bits) - 1u;
     const uint32_t base = part * kSortTile, cnt = min(kSortTile, K - base);
-    KeyT k[kItems];
-    uint32_t vr[kItems];
+    // kFull: a whole partition (all but the last), without per-key bounds
+    // checks and with a fixed write-out loop
+    auto partition = [&](auto full_tag) {
+        constexpr bool kFull = decltype(full_tag)::value;
+        KeyT k[kItems];
+        uint32_t vr[kItems];
 #pragma unroll
-    for (uint32_t i = 0; i < kItems; ++i) {
-        const uint32_t idx = warp * (kItems * 32) + i * 32 + lane;
-        k[i] = idx < cnt ? keys_in[base + idx] : KeyT(~KeyT(0));
-        vr[i] = idx < cnt ? vals_in[base + idx] : 0u;
-    }
-    // this partition's digit offsets: chunk base + offset within the chunk,
-    // written by the counting kernel (this kernel may have started while it
-    // ran: its keys and values come from the kernel before that one)
-    pdl_wait();
-    pdl_trigger();  // the next kernel (the next counting kernel, or the blend) may be scheduled; it waits for this grid
-    uint32_t goff = 0;
-    if (digit_thread) {
-        const uint32_t* chunk_rows = work + 256 * size_t(max_parts);
-        goff = ld_cg_u32(chunk_rows + size_t(part / kChunkParts) * 256 + tid) +
-               ld_cg_u32(work + size_t(part) * 256 + tid);
-    }
-#pragma unroll
-    for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
-    __syncthreads();
-    // stable rank within the warp (warp-striped order)
-    uint32_t dr[kItems];
-    const uint32_t lt = lanemask_lt();
-#pragma unroll
-    for (uint32_t i = 0; i < kItems; ++i) {
-        const uint32_t idx = warp * (kItems * 32) + i * 32 + lane;
-        const uint32_t d = idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
-        uint32_t peers = 0xFFFFFFFFu;
-#pragma unroll
-        for (int b = 0; b < kBits; ++b) {
-            const bool on = (d >> b) & 1u;
-            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
-            peers &= on ? bal : ~bal;
-        }
-        if (cnt < kSortTile) {
-            const bool on = d >= kRadix;
-            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
-            peers &= on ? bal : ~bal;
-        }
-        const uint32_t leader = __ffs(peers) - 1;
-        uint32_t prev = 0;
-        if (lane == leader && d < kRadix) {
-            prev = S.whist[warp][d];
-            S.whist[warp][d] = prev + __popc(peers);
-        }
-        prev = __shfl_sync(0xFFFFFFFFu, prev, leader);
-        dr[i] = d | ((prev + __popc(peers & lt)) << 9);
-        __syncwarp();
-    }
-    __syncthreads();
-    uint32_t count = 0;
-    if (digit_thread) {
-#pragma unroll
-        for (uint32_t w = 0; w < kWarps; ++w) {
-            const uint32_t c = S.whist[w][tid];
-            S.whist[w][tid] = count;
-            count += c;
-        }
-    }
-    const uint32_t lstart = block_exclusive_scan256<kWarps>(count, S.wsum);  // (its barriers cover whist)
-    if (digit_thread) {
-        S.lstart[tid] = lstart;
-        S.gmap[tid] = goff - lstart;
-    }
-    __syncthreads();
-#pragma unroll
-    for (uint32_t i = 0; i < kItems; ++i) {
-        const uint32_t d = dr[i] & 511u;
-        if (d < kRadix) {
-            const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
-            if (TPD_INBOUNDS(ctl, 20, pos, cnt)) {
-                S.keys[pad16(pos)] = k[i];
-                S.vals[pad16(pos)] = vr[i];
+        for (uint32_t i = 0; i < kItems; ++i) {
+            const uint32_t idx = warp * (kItems * 32) + i * 32 + lane;
+            if (kFull || idx < cnt) {
+                k[i] = keys_in[base + idx];
+                vr[i] = vals_in[base + idx];
+            } else {
+                k[i] = KeyT(~KeyT(0));
+                vr[i] = 0u;
             }
         }
-    }
-    __syncthreads();
-    for (uint32_t j = tid; j < cnt; j += kThreads) {
-        const KeyT key = S.keys[pad16(j)];
-        const uint32_t d = uint32_t(key >> shift) & mask;
-        const uint32_t g = S.gmap[d] + j;
-        if (g < capacity && TPD_INBOUNDS(ctl, 21, g, K + (K == 0))) {
-            keys_out[g] = key;
-            vals_out[g] = S.vals[pad16(j)];
-            if (ranges) tile_range_bounds(S, ranges, n_tiles, key, j, cnt, d, g, shift, mask, ctl);
+        // this partition's digit offsets: chunk base + offset within the chunk,
+        // written by the counting kernel (this kernel may have started while it
+        // ran: its keys and values come from the kernel before that one)
+        pdl_wait();
+        pdl_trigger();  // the next kernel (the next counting kernel, or the blend) may be scheduled; it waits for this grid
+        uint32_t goff = 0;
+        if (digit_thread) {
+            const uint32_t* chunk_rows = work + 256 * size_t(max_parts);
+            goff = ld_cg_u32(chunk_rows + size_t(part / kChunkParts) * 256 + tid) +
+                   ld_cg_u32(work + size_t(part) * 256 + tid);
         }
-    }
+#pragma unroll
+        for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
+        __syncthreads();
+        // stable rank within the warp (warp-striped order)
+        uint32_t dr[kItems];
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (uint32_t i = 0; i < kItems; ++i) {
+            const uint32_t idx = warp * (kItems * 32) + i * 32 + lane;
+            const uint32_t d = kFull || idx < cnt ? (uint32_t(k[i] >> shift) & mask) : kInvalidDigit;
+            uint32_t peers = 0xFFFFFFFFu;
+#pragma unroll
+            for (int b = 0; b < kBits; ++b) {
+                const bool on = (d >> b) & 1u;
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+                peers &= on ? bal : ~bal;
+            }
+            if constexpr (!kFull) {
+                const bool on = d >= kRadix;
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+                peers &= on ? bal : ~bal;
+            }
+            const uint32_t leader = __ffs(peers) - 1;
+            uint32_t prev = 0;
+            if (lane == leader && (kFull || d < kRadix)) {
+                prev = S.whist[warp][d];
+                S.whist[warp][d] = prev + __popc(peers);
+            }
+            prev = __shfl_sync(0xFFFFFFFFu, prev, leader);
+            dr[i] = d | ((prev + __popc(peers & lt)) << 9);
+            __syncwarp();
+        }
+        __syncthreads();
+        uint32_t count = 0;
+        if (digit_thread) {
+#pragma unroll
+            for (uint32_t w = 0; w < kWarps; ++w) {
+                const uint32_t c = S.whist[w][tid];
+                S.whist[w][tid] = count;
+                count += c;
+            }
+        }
+        const uint32_t lstart = block_exclusive_scan256<kWarps>(count, S.wsum);  // (its barriers cover whist)
+        if (digit_thread) {
+            S.lstart[tid] = lstart;
+            S.gmap[tid] = goff - lstart;
+        }
+        __syncthreads();
+#pragma unroll
+        for (uint32_t i = 0; i < kItems; ++i) {
+            const uint32_t d = dr[i] & 511u;
+            if (kFull || d < kRadix) {
+                const uint32_t pos = S.lstart[d] + S.whist[warp][d] + (dr[i] >> 9);
+                if (TPD_INBOUNDS(ctl, 20, pos, cnt)) {
+                    S.keys[pad16(pos)] = k[i];
+                    S.vals[pad16(pos)] = vr[i];
+                }
+            }
+        }
+        __syncthreads();
+        // (g < K <= capacity: the bound check covers the buffer's end)
+        auto write_out = [&](uint32_t j) {
+            const KeyT key = S.keys[pad16(j)];
+            const uint32_t d = uint32_t(key >> shift) & mask;
+            const uint32_t g = S.gmap[d] + j;
+            if (TPD_INBOUNDS(ctl, 21, g, K)) {
+                keys_out[g] = key;
+                vals_out[g] = S.vals[pad16(j)];
+                if (ranges) tile_range_bounds(S, ranges, n_tiles, key, j, cnt, d, g, shift, mask, ctl);
+            }
+        };
+        if constexpr (kFull) {
+#pragma unroll 4
+            for (uint32_t q = 0; q < kItems; ++q) write_out(tid + q * kThreads);
+        } else {
+            for (uint32_t j = tid; j < cnt; j += kThreads) write_out(j);
+        }
+    };
+    if (cnt == kSortTile)
+        partition(std::true_type{});
+    else
+        partition(std::false_type{});
 }
 
 // Residencies: the 256-thread, 16-key variant is compiled for 2 CTAs per SM
