@@ -262,49 +262,56 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
             // the update, so lanes taking different decisions do not run the
             // paths one after another. A skipped pair gets alpha = 0, which
             // leaves T and C exactly as they were.
-            while (m) {
-                const uint32_t jj = g + uint32_t(__ffs(m) - 1);
-                m &= m - 1u;
-                const PairStaged& E = S.e[b][jj];
-                const float4 xy = E.xy, qab = E.qab, qco = E.qco, rg = E.rg, bt = E.bt;
-                // p2 for both pixels
+            // alpha of a staged entry for both pixels (0 when the pair is skipped)
+            auto alpha_of = [&](const PairStaged& E) {
+                const float4 xy = E.xy, qab = E.qab, qco = E.qco, bt = E.bt;
                 const float2 dx = __fadd2_rn(make_float2(xy.x, xy.y), npx);
                 const float2 dy = __fadd2_rn(make_float2(xy.z, xy.w), npy);
                 const float2 t = __ffma2_rn(make_float2(qab.z, qab.w), dy, __fmul2_rn(make_float2(qab.x, qab.y), dx));
                 const float2 p2 = __ffma2_rn(t, dx, __fmul2_rn(__fmul2_rn(make_float2(qco.x, qco.y), dy), dy));
                 const float2 ao =
                     __fmul2_rn(make_float2(qco.z, qco.w), make_float2(ex2_approx(p2.x), ex2_approx(p2.y)));
+                return make_float2(pair_skipped(p2.x, bt.z) ? 0.0f : fminf(kAlphaMax, ao.x),
+                                   pair_skipped(p2.y, bt.z) ? 0.0f : fminf(kAlphaMax, ao.y));
+            };
+            // the pair's update, in list order. keep = 0 at the stop and after
+            // it (T = 0 gives tn = 0): the pair adds alpha T * 0 = 0 and T
+            // becomes 0; before the stop keep = 1 and both products are exact
+            // copies. With the adjoint's inputs, Tk keeps the transmittance at
+            // the stop and the last entry that added is the last with w > 0
+            // (alpha >= 1/255 times T >= 1e-4).
+            auto apply = [&](float2 alpha, const PairStaged& E, uint32_t jj) {
+                const float4 rg = E.rg, bt = E.bt;
+                const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
+                const bool go_a = !(tn.x < kTMin), go_b = !(tn.y < kTMin);
+                const float2 keep = make_float2(go_a ? 1.0f : 0.0f, go_b ? 1.0f : 0.0f);
+                const float2 w = __fmul2_rn(__fmul2_rn(alpha, T), keep);
+                C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
+                C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
+                C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
+                T = __fmul2_rn(tn, keep);
                 if constexpr (kState) {
-                    // the frozen form below, plus Tk, the transmittance as the
-                    // reference keeps it (it stays at the stop), and the last
-                    // entry that added: w > 0 exactly when the pair adds
-                    // (alpha >= 1/255 times T >= 1e-4)
-                    const float2 alpha = make_float2(pair_skipped(p2.x, bt.z) ? 0.0f : fminf(kAlphaMax, ao.x),
-                                                     pair_skipped(p2.y, bt.z) ? 0.0f : fminf(kAlphaMax, ao.y));
-                    const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
-                    const bool go_a = !(tn.x < kTMin), go_b = !(tn.y < kTMin);
-                    const float2 keep = make_float2(go_a ? 1.0f : 0.0f, go_b ? 1.0f : 0.0f);
-                    const float2 w = __fmul2_rn(__fmul2_rn(alpha, T), keep);
-                    C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
-                    C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
-                    C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
-                    T = __fmul2_rn(tn, keep);
                     Tk = make_float2(go_a ? tn.x : Tk.x, go_b ? tn.y : Tk.y);
                     last_a = w.x > 0.0f ? lbase + jj : last_a;
                     last_b = w.y > 0.0f ? lbase + jj : last_b;
+                }
+            };
+            // without the adjoint's inputs, two entries per step when there are
+            // two: their alphas are independent, only the updates run in order
+            // (with them, the extra registers cost more than the overlap gives)
+            while (m) {
+                const uint32_t j0 = g + uint32_t(__ffs(m) - 1);
+                m &= m - 1u;
+                if (!kState && m) {
+                    const uint32_t j1 = g + uint32_t(__ffs(m) - 1);
+                    m &= m - 1u;
+                    const PairStaged &E0 = S.e[b][j0], &E1 = S.e[b][j1];
+                    const float2 a0 = alpha_of(E0), a1 = alpha_of(E1);
+                    apply(a0, E0, j0);
+                    apply(a1, E1, j1);
                 } else {
-                    // keep = 0 at the stop and after it (T = 0 gives tn = 0):
-                    // the pair adds alpha T * 0 = 0 and T becomes 0; before
-                    // the stop keep = 1 and both products are exact copies
-                    const float2 alpha = make_float2(pair_skipped(p2.x, bt.z) ? 0.0f : fminf(kAlphaMax, ao.x),
-                                                     pair_skipped(p2.y, bt.z) ? 0.0f : fminf(kAlphaMax, ao.y));
-                    const float2 tn = __fmul2_rn(T, __ffma2_rn(mone, alpha, one));  // T (1 - alpha)
-                    const float2 keep = make_float2(tn.x < kTMin ? 0.0f : 1.0f, tn.y < kTMin ? 0.0f : 1.0f);
-                    const float2 w = __fmul2_rn(__fmul2_rn(alpha, T), keep);
-                    C0 = __ffma2_rn(make_float2(rg.x, rg.y), w, C0);
-                    C1 = __ffma2_rn(make_float2(rg.z, rg.w), w, C1);
-                    C2 = __ffma2_rn(make_float2(bt.x, bt.y), w, C2);
-                    T = __fmul2_rn(tn, keep);
+                    const PairStaged& E0 = S.e[b][j0];
+                    apply(alpha_of(E0), E0, j0);
                 }
             }
         }
