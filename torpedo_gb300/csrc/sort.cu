@@ -21,9 +21,13 @@
 //     memory while predecessors publish, resolves each digit's global prefix
 //     by a decoupled look-back (one thread per digit, four predecessors per
 //     round trip, bounded spin) and writes digit runs out coalesced.
-// In the frame the depth presort sorts 64-bit (view | depth) keys and the key
-// sort 32-bit tile ids (their depth order is already fixed); the standalone
-// sort takes 64-bit keys.
+//  3. Counted passes (the frame's key sort, below): a counting kernel, then a
+//     scatter kernel per pass, with every partition's digit offsets known
+//     before it scatters, so no partition waits on another.
+// In the frame the depth presort sorts 64-bit (view | depth) keys with
+// onesweep passes and the key sort 32-bit tile ids (their depth order is
+// already fixed) with counted passes; the standalone sort takes 64-bit keys
+// (onesweep, 256 threads x 16 keys).
 // The result is the stable sort of the pairs by the low key_bits bits, the
 // same permutation as the reference's sort.
 #include <algorithm>
@@ -48,7 +52,8 @@ constexpr uint32_t kInvalidDigit = kRadix;                  // keys past K (and 
 
 // Pass kinds of onesweep_kernel. The depth sort compacts the culled items
 // away in its first pass and sorts the remaining ctl->depth_count items in
-// the others, where a pass whose digit is the same for every key is a copy.
+// the others, where a pass whose digit is the same for every key is skipped
+// (counted in ctl->depth_skips; the later passes swap their buffers).
 constexpr int kPassPlain = 0;      // K = fixed_count, else ctl->total_keys
 constexpr int kPassDropCulled = 1; // as plain; keys whose low 32 bits are 0xFFFFFFFF are not written
 constexpr int kPassCompacted = 2;  // K = ctl->depth_count; a uniform digit skips the pass (ctl->depth_skips)
