@@ -128,6 +128,15 @@ __device__ __forceinline__ float ex2_approx(float x) {
     return y;
 }
 
+// UNORM RGBA8 of (r, g, b, 1): round(clamp(c, 0, 1) * 255) per channel.
+__device__ __forceinline__ uint32_t rgba8_unorm(float r, float g, float b) {
+    const float c[3] = {r, g, b};
+    uint32_t out = 0xFF000000u;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) out |= uint32_t(__float2uint_rn(fminf(fmaxf(c[k], 0.0f), 1.0f) * 255.0f)) << (8 * k);
+    return out;
+}
+
 // true when the pair is skipped (power > 0 or alpha < 1/255)
 __device__ __forceinline__ bool pair_skipped(float p2, float thr) { return p2 > 0.0f || p2 < thr; }
 
@@ -324,6 +333,7 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
             a.image[p * 3 + 0] = C0.x;
             a.image[p * 3 + 1] = C1.x;
             a.image[p * 3 + 2] = C2.x;
+            if (a.rgba) a.rgba[p] = rgba8_unorm(C0.x, C1.x, C2.x);
             if constexpr (kState) {
                 a.final_T[p] = Tk.x;
                 a.n_contrib[p] = last_a;
@@ -334,6 +344,7 @@ __device__ __forceinline__ void blend_tile(const BlendArgs& a, uint32_t tile, Fw
             a.image[p * 3 + 0] = C0.y;
             a.image[p * 3 + 1] = C1.y;
             a.image[p * 3 + 2] = C2.y;
+            if (a.rgba) a.rgba[p] = rgba8_unorm(C0.y, C1.y, C2.y);
             if constexpr (kState) {
                 a.final_T[p] = Tk.y;
                 a.n_contrib[p] = last_b;
@@ -381,13 +392,7 @@ __global__ void pack_rgba8_kernel(const float* rgb, uint32_t* rgba, size_t pixel
     pdl_trigger();
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= pixels) return;
-    uint32_t out = 0xFF000000u;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float v = fminf(fmaxf(rgb[i * 3 + c], 0.0f), 1.0f);
-        out |= uint32_t(__float2uint_rn(v * 255.0f)) << (8 * c);
-    }
-    rgba[i] = out;
+    rgba[i] = rgba8_unorm(rgb[i * 3 + 0], rgb[i * 3 + 1], rgb[i * 3 + 2]);
 }
 
 constexpr int kG2D = 9;  // px, py, conic.x, conic.y, conic.z, opacity, r, g, b

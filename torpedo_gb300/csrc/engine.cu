@@ -159,7 +159,6 @@ struct tpd_engine {
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
     bool graph_state = false;      // the frame graph keeps the adjoint's inputs
-    bool body_graph_state = false; // the same for the pipelined renders' graph
     bool state_kept = false;       // the last frame kept them (final T, last contributor)
     bool backward_seen = false;    // tpd_backward has been called on this engine
     bool needs_eager = true;  // the first frame after any change runs without a graph
@@ -175,7 +174,12 @@ struct tpd_engine {
     // device staging image and completion events; the image copy to the
     // caller runs on copy_stream, so the next frame computes meanwhile
     static constexpr int kRing = 2;
-    cudaGraphExec_t body_graph = nullptr;  // the frame without uploads and stats copy
+    // per slot and image format (RGBA8, RGB32F): the slot's upload of the
+    // view constants (and transforms), the frame, its image into the slot's
+    // staging buffer (the blend writes RGBA8 itself) and the stats copy
+    cudaGraphExec_t slot_graph[kRing][2] = {};
+    bool slot_graph_state[kRing][2] = {};  // captured keeping the adjoint's inputs
+    bool slot_graph_ident[kRing][2] = {};  // captured without transforms
     cudaStream_t copy_stream = nullptr;
     ViewConst* ring_views[kRing] = {};
     float* ring_transforms[kRing] = {};
@@ -219,14 +223,21 @@ void invalidate_step_graph(tpd_engine* e) {
     for (auto& k : e->step_key) k = nullptr;
 }
 
+void invalidate_slot_graphs(tpd_engine* e) {
+    for (auto& row : e->slot_graph)
+        for (auto& g : row) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
 void invalidate_graph(tpd_engine* e) {
     if (e->graph) cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;
     e->graph_valid = false;
     e->needs_eager = true;
     invalidate_step_graph(e);
-    if (e->body_graph) cudaGraphExecDestroy(e->body_graph);
-    e->body_graph = nullptr;
+    invalidate_slot_graphs(e);
 }
 
 // Views x n sized buffers.
@@ -337,8 +348,9 @@ BlendLaunch blend_launch(const tpd_engine* e) {
 // Enqueues one frame on the stream (no host synchronisation).
 // io = false leaves out the uploads of the view constants and transforms and
 // the stats copy (the pipelined renders enqueue those per slot).
-// state: the blend also keeps the adjoint's inputs (final T, last contributor).
-void enqueue_frame(tpd_engine* e, bool io = true, bool state = true) {
+// state: the blend also keeps the adjoint's inputs (final T, last contributor);
+// rgba: non-null, the blend also writes the image there as RGBA8.
+void enqueue_frame(tpd_engine* e, bool io = true, bool state = true, uint32_t* rgba = nullptr) {
     cudaStream_t s = e->stream;
     cudaEvent_t* ev = nullptr;
     if (e->settings.stage_timing) {
@@ -458,6 +470,7 @@ void enqueue_frame(tpd_engine* e, bool io = true, bool state = true) {
     ba.image_offset = e->n_views > 1 ? e->d_image_offset : nullptr;
     ba.final_T = state ? e->d_final_T : nullptr;
     ba.n_contrib = state ? e->d_n_contrib : nullptr;
+    ba.rgba = rgba;
     launch_blend(ba, blend_launch(e), s);
     mark(6);
     // the backward stages of a frame without backward take no time; a
@@ -642,6 +655,7 @@ int ensure_ring(tpd_engine* e) {
         }
     }
     if (!e->identity_transforms && e->n_ent > e->ring_transforms_cap) {
+        invalidate_slot_graphs(e);  // they read the old buffers
         for (int i = 0; i < tpd_engine::kRing; ++i) {
             if (e->ring_transforms[i]) cudaFreeHost(e->ring_transforms[i]);
             e->ring_transforms[i] = nullptr;
@@ -651,6 +665,7 @@ int ensure_ring(tpd_engine* e) {
     }
     const uint64_t bytes = e->total_pixels * 12;  // room for RGB32F
     if (bytes > e->ring_image_cap) {
+        invalidate_slot_graphs(e);
         for (int i = 0; i < tpd_engine::kRing; ++i) TPD_CUDA(e, dalloc(e->ring_image[i], bytes));
         e->ring_image_cap = bytes;
     }
@@ -964,51 +979,50 @@ int tpd_render_async(tpd_engine* e, void* dst, uint32_t format, int dst_is_devic
         return fail(e, TPD_ERR_STATE, "the views grew while renders are outstanding: call tpd_wait_render first");
     }
     cudaStream_t s = e->stream;
-    // the frame's constants, snapshotted into the slot (its last render has been waited for)
+    // the frame's constants, snapshotted into the slot (its last render has
+    // been waited for); the slot's upload reads them when it runs
     std::memcpy(e->ring_views[slot], e->h_views, sizeof(ViewConst) * e->n_views);
-    TPD_CUDA(e, cudaMemcpyAsync(e->d_views, e->ring_views[slot], sizeof(ViewConst) * e->n_views,
-                                cudaMemcpyHostToDevice, s));
-    if (!e->identity_transforms) {
+    if (!e->identity_transforms)
         std::memcpy(e->ring_transforms[slot], e->h_transforms, sizeof(float) * 16 * e->n_ent);
-        TPD_CUDA(e, cudaMemcpyAsync(e->d_transforms, e->ring_transforms[slot], sizeof(float) * 16 * e->n_ent,
-                                    cudaMemcpyHostToDevice, s));
-    }
-    const bool graph = e->settings.use_graph && !e->settings.stage_timing;
+    const int f = format == TPD_IMAGE_RGBA8 ? 0 : 1;
+    const uint64_t bytes = format == TPD_IMAGE_RGBA8 ? e->total_pixels * 4 : e->total_pixels * 12;
     const bool state = frame_state(e);
+    auto enqueue_slot = [&]() {
+        cudaMemcpyAsync(e->d_views, e->ring_views[slot], sizeof(ViewConst) * e->n_views, cudaMemcpyHostToDevice, s);
+        if (!e->identity_transforms)
+            cudaMemcpyAsync(e->d_transforms, e->ring_transforms[slot], sizeof(float) * 16 * e->n_ent,
+                            cudaMemcpyHostToDevice, s);
+        enqueue_frame(e, false, state, f == 0 ? reinterpret_cast<uint32_t*>(e->ring_image[slot]) : nullptr);
+        if (f == 1) cudaMemcpyAsync(e->ring_image[slot], e->d_image, bytes, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(e->ring_stats[slot], e->d_ctl, sizeof(StatsHead), cudaMemcpyDeviceToHost, s);
+    };
+    const bool graph = e->settings.use_graph && !e->settings.stage_timing;
     if (graph) {
-        if (e->body_graph && e->body_graph_state != state) {
-            cudaGraphExecDestroy(e->body_graph);
-            e->body_graph = nullptr;
+        cudaGraphExec_t& G = e->slot_graph[slot][f];
+        if (G && (e->slot_graph_state[slot][f] != state || e->slot_graph_ident[slot][f] != e->identity_transforms)) {
+            cudaGraphExecDestroy(G);
+            G = nullptr;
         }
-        if (!e->body_graph) {
+        if (!G) {
             cudaGraph_t g = nullptr;
             TPD_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            enqueue_frame(e, false, state);
+            enqueue_slot();
             TPD_CUDA(e, cudaStreamEndCapture(s, &g));
             cudaGraphExec_t ge = nullptr;
             const cudaError_t err = cudaGraphInstantiate(&ge, g, 0);
             cudaGraphDestroy(g);
             TPD_CUDA(e, err);
-            e->body_graph = ge;
-            e->body_graph_state = state;
+            G = ge;
+            e->slot_graph_state[slot][f] = state;
+            e->slot_graph_ident[slot][f] = e->identity_transforms;
         }
         before_frame(e);
-        TPD_CUDA(e, cudaGraphLaunch(e->body_graph, s));
+        TPD_CUDA(e, cudaGraphLaunch(G, s));
     } else {
         before_frame(e);
-        enqueue_frame(e, false, state);
+        enqueue_slot();
     }
     e->state_kept = state;
-    // image into the slot's staging buffer and stats into its pinned slot
-    uint64_t bytes;
-    if (format == TPD_IMAGE_RGBA8) {
-        launch_pack_rgba8(e->d_image, reinterpret_cast<uint32_t*>(e->ring_image[slot]), e->total_pixels, s);
-        bytes = e->total_pixels * 4;
-    } else {
-        TPD_CUDA(e, cudaMemcpyAsync(e->ring_image[slot], e->d_image, e->total_pixels * 12, cudaMemcpyDeviceToDevice, s));
-        bytes = e->total_pixels * 12;
-    }
-    TPD_CUDA(e, cudaMemcpyAsync(e->ring_stats[slot], e->d_ctl, sizeof(StatsHead), cudaMemcpyDeviceToHost, s));
     TPD_CUDA(e, cudaEventRecord(e->ring_ready[slot], s));
     // the caller's copy runs beside the next frame
     TPD_CUDA(e, cudaStreamWaitEvent(e->copy_stream, e->ring_ready[slot], 0));

@@ -182,6 +182,9 @@ struct BlendArgs {
     // contributor (the adjoint's inputs); both null: not tracked
     float* final_T;
     uint32_t* n_contrib;
+    // nullable: the image also as RGBA8 UNORM (alpha 255), packed like image
+    // (launch_pack_rgba8's conversion), written with it
+    uint32_t* rgba;
 };
 // Launch settings of the blend and its adjoint: list entries per staged
 // round (forward 64 / 128 / 256, adjoint 32 / 64 / 128) and the form of the
