@@ -76,7 +76,8 @@ typedef struct tpd_settings {
     uint32_t sort_ctas_per_sm;     /* residency of the 256 x 16-key radix pass kernels: 2 (0 = default, no register spills) or 3;
                                       for the counted key sort 3 (0 = default) or 2 */
     uint32_t depth_sort_items;     /* keys per thread of the depth sort's 256-thread radix passes: 16 (0 = default), 8 or 4 */
-    uint32_t sort_threads;         /* CTA size of the key sort's 4096-key radix passes: 512 x 8 keys (0 = default) or 256 x 16 */
+    uint32_t sort_threads;         /* CTA size of the key sort's onesweep passes (key_sort_lookback = 1): 512 x 8 keys
+                                      (0 = default) or 256 x 16; the counted passes run 256 x 16 */
     uint32_t depth_sort_threads;   /* CTA size of the depth sort's radix passes: 256 (0 = default) or 512 (8 keys each,
                                       whatever depth_sort_items says) */
     uint32_t blend_round;          /* list entries the blend stages per round: 128 (0 = default), 64 or 256 */

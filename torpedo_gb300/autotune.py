@@ -12,7 +12,9 @@ result bit for bit unchanged:
                      with a decoupled look-back (1)
   sort_threads       CTA size of the onesweep key sort's 4096-key passes: 512
                      threads x 8 keys (digits ranked with match-any, twice the
-                     warps per SM) or 256 threads x 16 keys (bit ballots)
+                     warps per SM) or 256 threads x 16 keys (bit ballots);
+                     tried only with key_sort_lookback = 1 (the counted
+                     passes always run 256 x 16 keys)
   depth_sort_threads the same choice for the depth sort's passes
   depth_sort_items   keys per thread of the depth sort's 256-thread passes
                      (16, 8, 4: partitions of 4096, 2048, 1024 keys); smaller
@@ -43,6 +45,8 @@ from typing import Callable
 AXES = (("key_sort_lookback", (0, 1)), ("sort_threads", (256, 512)), ("depth_sort_threads", (256, 512)),
         ("depth_sort_items", (16, 8)), ("sort_ctas_per_sm", (0, 2)))
 TRAIN_AXES = (("blend_backward_round", (64, 32, 128)), ("blend_round", (128, 64, 256)), ("blend_persistent", (0, 1)))
+# axes that change nothing under the given settings: not tried there
+INERT = {"sort_threads": lambda s: s.get("key_sort_lookback", 0) == 0}
 
 
 def time_steps(make_engine: Callable[[dict], object], enqueue: Callable[[object, int], None], stream,
@@ -74,6 +78,8 @@ def tune(make_engine: Callable[[dict], object], enqueue: Callable[[object, int],
     results: dict[str, float] = {}
     best_ms = None
     for name, values in axes:
+        if name in INERT and INERT[name](best):
+            continue
         for v in values:
             cand = dict(best, **{name: v})
             label = ",".join(f"{k}={x}" for k, x in cand.items() if k in dict(axes))
