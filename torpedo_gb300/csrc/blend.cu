@@ -185,9 +185,8 @@ struct FwdStage {
     uint8_t mask[2][kRound];  // bit w: the entry can reach warp w's 8x8 block
 };
 
-__device__ __forceinline__ void stage_pair_entry(const Splat* sp, float ox, float oy, PairStaged& d, uint8_t& mask) {
-    const float4* p = reinterpret_cast<const float4*>(sp);
-    const float4 c = __ldg(p + 0), tex = __ldg(p + 1), co = __ldg(p + 2);
+__device__ __forceinline__ void stage_pair_values(float4 c, float4 tex, float4 co, float ox, float oy, PairStaged& d,
+                                                  uint8_t& mask) {
     const float thr = co.w > 0.0f ? -__log2f(255.0f * co.w) : kInf;  // +inf: never blends
     const float4 q = make_float4(-0.5f * kLog2e * co.x, -kLog2e * co.y, -0.5f * kLog2e * co.z, thr);
     d.xy = make_float4(tex.x, tex.x, tex.y, tex.y);
@@ -196,6 +195,11 @@ __device__ __forceinline__ void stage_pair_entry(const Splat* sp, float ox, floa
     d.rg = make_float4(c.x, c.x, c.y, c.y);
     d.bt = make_float4(c.z, c.z, thr, 0.0f);
     mask = uint8_t(block_mask<2>(tex.x, tex.y, q, ox, oy));
+}
+
+__device__ __forceinline__ void stage_pair_entry(const Splat* sp, float ox, float oy, PairStaged& d, uint8_t& mask) {
+    const float4* p = reinterpret_cast<const float4*>(sp);
+    stage_pair_values(__ldg(p + 0), __ldg(p + 1), __ldg(p + 2), ox, oy, d, mask);
 }
 
 __device__ __forceinline__ void stage_pair_empty(PairStaged& d, uint8_t& mask) {
@@ -520,12 +524,41 @@ __device__ __forceinline__ void blend_backward_tile(const BlendBackwardArgs& a, 
     };
     if (max_last > 0) stage_round(int32_t(max_last), 0, 0);
     __syncthreads();
+    // the next round's entry of this thread (one per thread: kBwdRound <=
+    // kFwdThreads), loaded before the current round is walked and staged after
+    // it, so the gathers' latency hides behind the walk
+    static_assert(kBwdRound <= kFwdThreads, "one staged entry per thread");
+    bool pf = false;
+    uint32_t pf_idx = 0;
+    float4 pf_c = make_float4(0.f, 0.f, 0.f, 0.f), pf_tex = pf_c, pf_co = pf_c;
+    auto load_next = [&](int32_t r_end) {
+        pf = tid < uint32_t(min(int32_t(kBwdRound), r_end));
+        if (!pf) return;
+        pf_idx = a.vals[start + uint32_t(r_end) - 1u - tid];
+        if (pf_idx < a.n) {
+            const float4* p = reinterpret_cast<const float4*>(vsplats + pf_idx);
+            pf_c = __ldg(p + 0);
+            pf_tex = __ldg(p + 1);
+            pf_co = __ldg(p + 2);
+        }
+    };
+    auto store_next = [&](uint32_t b, uint32_t bi) {
+        if (!pf) return;
+        if (pf_idx < a.n) {
+            stage_pair_values(pf_c, pf_tex, pf_co, ox, oy, SM.e[b][tid], SM.mask[b][tid]);
+        } else {  // only reachable with corrupted lists
+            pf_idx = 0;
+            stage_pair_empty(SM.e[b][tid], SM.mask[b][tid]);
+        }
+        SM.idx[bi][tid] = pf_idx;
+    };
     const float2 one = f2(1.0f, 1.0f), mone = f2(-1.0f, -1.0f), mhalf = f2(-0.5f, -0.5f), ln2 = f2(kLn2, kLn2);
     uint32_t r = 0;
     for (int32_t r_end = int32_t(max_last); r_end > 0; r_end -= int32_t(kBwdRound), ++r) {
         const uint32_t b = r & 1u, bi = r % 3u;
         const uint32_t n = uint32_t(min(int32_t(kBwdRound), r_end));
-        if (r_end > int32_t(kBwdRound)) stage_round(r_end - int32_t(kBwdRound), b ^ 1u, (r + 1) % 3u);
+        if (r_end > int32_t(kBwdRound)) load_next(r_end - int32_t(kBwdRound));
+        else pf = false;
         // entries jj >= skip have list positions r_end - 1 - jj below warp_last
         const uint32_t skip = uint32_t(r_end) > warp_last ? uint32_t(r_end) - warp_last : 0u;
         for (uint32_t g = skip & ~31u; g < n; g += 32) {
@@ -596,6 +629,7 @@ __device__ __forceinline__ void blend_backward_tile(const BlendBackwardArgs& a, 
                 }
             }
         }
+        store_next(b ^ 1u, (r + 1) % 3u);
         __syncthreads();  // round r's sums complete; the other stage buffer is filled
         // one 16-byte vector atomic per non-zero quarter of an entry's record;
         // the thread that adds a quarter also zeroes it for round r + 2
