@@ -101,13 +101,25 @@ __global__ void __launch_bounds__(kBwdThreads) preprocess_backward_kernel(Prepro
 #pragma unroll
     for (int k = 0; k < 48; ++k) gsh[k] = 0.f;
 
-    for (uint32_t v = 0; v < a.n_views && active; ++v) {
-        // the splat (colour, tiles | texel | conic, opacity) and its gradient record, 16 bytes at a time
+    // the splat (colour, tiles | texel | conic, opacity) and its gradient
+    // record of view v, 16 bytes at a time; view v + 1's are loaded while
+    // view v is worked on (a gradient record is read whether or not the
+    // Gaussian is visible in that view: it is zero then)
+    float4 n_c, n_t, n_g0, n_g1, n_g2;
+    auto load_view = [&](uint32_t v) {
         const float4* sp4 = reinterpret_cast<const float4*>(a.splats + size_t(v) * a.n + i);
-        const float4 sp_c = sp4[0], sp_t = sp4[1];
-        if (!(sp_t.w > 0.0f)) continue;
+        n_c = sp4[0];
+        n_t = sp4[1];
         const float4* g4 = reinterpret_cast<const float4*>(a.g2d + (size_t(v) * a.n + i) * kG2DStride);
-        const float4 ga4 = g4[0], gb4 = g4[1], gc4 = g4[2];
+        n_g0 = g4[0];
+        n_g1 = g4[1];
+        n_g2 = g4[2];
+    };
+    if (active && a.n_views) load_view(0);
+    for (uint32_t v = 0; v < a.n_views && active; ++v) {
+        const float4 sp_c = n_c, sp_t = n_t, ga4 = n_g0, gb4 = n_g1, gc4 = n_g2;
+        if (v + 1 < a.n_views) load_view(v + 1);
+        if (!(sp_t.w > 0.0f)) continue;
         const float g[9] = {ga4.x, ga4.y, ga4.z, ga4.w, gb4.x, gb4.y, gb4.z, gb4.w, gc4.x};
         const ViewConst& vc = a.views[v];
         const float* em = a.ent_mats + (size_t(v) * a.n_ent + e) * kEntityMatFloats;
