@@ -268,3 +268,56 @@ def test_render_async_pipelined_matches_synchronous(cuda):
         last = ref[order[-1]][0 if rgba else 1]
         np.testing.assert_array_equal(got.reshape(last.shape), last)
     eng.close()
+
+
+def test_render_async_views_and_transforms(cuda):
+    """Pipelined renders of three views of mixed sizes with per-entity model
+    matrices, the matrices changed between renders: each slot's captured
+    graph uploads its own views and transforms and the blend writes the
+    RGBA8 image itself, bit for bit the synchronous frames' packed images."""
+    torch = cuda
+    recs = configs.scene("cfg0", 6000).records
+    ent = (np.arange(len(recs)) % 3).astype(np.uint32)
+    c, s = np.cos(0.3), np.sin(0.3)
+    tr_a = np.stack([np.eye(4, dtype=np.float32),
+                     np.array([[c, 0, s, 0.2], [0, 1, 0, -0.1], [-s, 0, c, 0.4], [0, 0, 0, 1]], np.float32),
+                     np.array([[1, 0, 0, 0], [0, 1, 0, -1.0], [0, 0, 1, -0.5], [0, 0, 0, 1]], np.float32)])
+    tr_b = tr_a.copy()
+    tr_b[1, 0, 3] = -0.3
+    cams = [T.Camera.orbit((1.0, -0.5, -4.5), 320, 240), T.Camera.orbit((-0.8, 0.3, -4.0), 173, 91),
+            T.Camera.orbit((0.2, 0.9, -4.8), 256, 256)]
+
+    def make():
+        e = T.GaussianEngine()
+        e.compile(recs, ent, 3)
+        e.set_views(cams)
+        return e
+
+    ref = {}
+    for name, tr in (("a", tr_a), ("b", tr_b)):
+        e = make()
+        for k, m in enumerate(tr):
+            e.transform_host.transform(k, m)
+        e.raster_frame()
+        ref[name] = [img.copy() for img in e.read_image(rgba8=True)]
+        e.close()
+    eng = make()
+    for k, m in enumerate(tr_a):
+        eng.transform_host.transform(k, m)
+    eng.raster_frame()
+    px = sum(cm.width * cm.height for cm in cams)
+    host = [torch.zeros(px * 4, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    order = ["a", "b", "b", "a"]
+    for i, name in enumerate(order):
+        for k, m in enumerate(tr_a if name == "a" else tr_b):
+            eng.transform_host.transform(k, m)
+        eng.render_async(host[i % 2], rgba8=True)
+        if i >= 1:
+            assert eng.wait_render()["status"] == 0
+            got, off = host[(i - 1) % 2].cpu().numpy(), 0
+            for cm, want in zip(cams, ref[order[i - 1]]):
+                n = cm.width * cm.height * 4
+                np.testing.assert_array_equal(got[off:off + n].reshape(want.shape), want)
+                off += n
+    eng.wait_render()
+    eng.close()
