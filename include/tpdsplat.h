@@ -98,8 +98,8 @@ typedef struct tpd_settings {
 /* Stages of a frame (and of a training step), for tpd_stage_times. */
 enum {
     TPD_STAGE_PREPROCESS = 0, /* camera upload, entity matrices, preprocess (splats + depth keys) */
-    TPD_STAGE_DEPTH_SORT = 1, /* radix sort of the (view | depth) keys, tile-count scan in depth order */
-    TPD_STAGE_KEYGEN = 2,     /* key duplication in depth order */
+    TPD_STAGE_DEPTH_SORT = 1, /* radix sort of the (view | depth) keys */
+    TPD_STAGE_KEYGEN = 2,     /* tile-count scan and key duplication in depth order (one kernel) */
     TPD_STAGE_KEY_SORT = 3,   /* radix sort of the (tile | depth) keys on their tile-id bits */
     TPD_STAGE_RANGES = 4,     /* empty: the key sort's last pass writes the tile ranges */
     TPD_STAGE_BLEND = 5,      /* alpha blend */

@@ -256,7 +256,7 @@ int ensure_splat_buffers(tpd_engine* e) {
         TPD_CUDA(e, cudaMemset(e->d_desc_depth, 0, de * 8));
         e->splat_cap = need;
     }
-    const uint64_t parts = need / kScanTileStandalone + 2;
+    const uint64_t parts = need / std::min(kScanTileStandalone, kKeygenPart) + 2;  // the frame's scan partitions
     if (parts > e->desc_pre_cap) {
         invalidate_graph(e);
         TPD_CUDA(e, dalloc(e->d_desc_pre, parts));
@@ -427,12 +427,11 @@ void enqueue_frame(tpd_engine* e, bool io = true, bool state = true, uint32_t* r
     // the order is in the other buffer when a pass skipped (ctl->depth_skips odd)
     const uint32_t* order = e->d_ditems[e->depth_in_alt ? 1 : 0];
     const uint32_t* order_other = e->d_ditems[e->depth_in_alt ? 0 : 1];
-    launch_depth_scan(e->d_splats, order, order_other, items, e->d_offsets, e->d_desc_pre, e->d_ctl, spin,
-                      e->settings.test_never_publish, s);
     mark(2);
     const uint32_t cap = uint32_t(e->capacity);
-    launch_keygen(e->d_splats, order, order_other, e->d_offsets, items, e->n, e->d_views, e->d_tiles[0], e->d_vals[0],
-                  cap, e->key_bits, e->d_ranges, e->total_tiles, e->d_ctl, e->num_sms, s);
+    launch_keygen_scan(e->d_splats, order, order_other, items, e->n, e->d_views, e->d_offsets, e->d_tiles[0],
+                       e->d_vals[0], cap, e->d_ranges, e->total_tiles, e->d_desc_pre, e->d_ctl, spin,
+                       e->settings.test_never_publish, e->num_sms, s);
     mark(3);
     SortPlan kp;
     kp.first_bit = 0;  // tile ids; the depth half of the keys is already in order

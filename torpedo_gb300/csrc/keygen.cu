@@ -23,23 +23,16 @@ namespace tpd {
 namespace {
 
 constexpr uint32_t kKeygenThreads = 256;
+constexpr uint32_t kKeygenChunks = kKeygenPart / kKeygenThreads;  // 32-item chunks per warp and partition
+static_assert(kKeygenChunks * kKeygenThreads == kKeygenPart, "a partition is whole chunks of every warp");
 
-// Walks the ctl->depth_count (view, Gaussian) items the depth sort kept, in
-// depth order (items[r] = v * n + i < n_items, their key offsets in
-// offsets[r]); a warp owns 32 consecutive items, whose keys
-// are contiguous, and produces them in windows of kKeyWindow output slots:
+// A warp writes the keys of 32 consecutive items (one per lane), whose keys
+// are contiguous, in windows of kKeyWindow output slots:
 //  1. each lane with keys marks its first slot in the window's owner map,
 //     a prefix-max over the map gives every slot its owning lane;
 //  2. lane l fills slots l, l + 32, ...: owner's rectangle from a per-warp
 //     table, (row, column) of the slot's index inside the rectangle, the key,
 //     one coalesced store of key and value.
-// A key is stored as its tile id alone: the low 32 bits of the reference's
-// key are the depth, already in order (the items come in depth order), and
-// the depth of a key is that of its value's splat, so the sort needs only the
-// tile ids and the full keys can be rebuilt from (tile, value) when read.
-// Keys past the capacity are not written (the frame is flagged and rendered
-// again). The digit counts of the tile ids come from the preprocess, which
-// counts each Gaussian's tile rectangle row by row.
 constexpr uint32_t kKeyWindow = 256;
 constexpr uint32_t kKeygenWarps = kKeygenThreads / 32;
 
@@ -51,166 +44,237 @@ struct KeygenSmem {
     uint32_t gi[kKeygenWarps][32];             // Gaussian index
 };
 
+// Per item of a warp's 32 (one per lane): the first tile of its rectangle (t0,
+// row-major in its view), the rectangle's width and the view's grid width
+// (wgx = w | gx << 16), its key count (w h) and Gaussian index.
+struct ItemRect {
+    uint32_t t0, wgx, cnt, gi;
+};
+
+__device__ __forceinline__ ItemRect item_rect(uint32_t item, bool valid, float4 texel, uint32_t n_items, uint32_t n,
+                                              const ViewConst* __restrict__ views, FrameCtl* ctl) {
+    uint32_t w = 1, h = 0, gx = 1, gi = 0, t0 = 0;
+    if (valid && TPD_INBOUNDS(ctl, 21, item, n_items)) {
+        const uint32_t v = n_items == n ? 0u : item / n;  // one view: no division
+        gi = item - v * n;
+        const ViewConst& vc = views[v];
+        gx = grid_x(vc.width);
+        if (texel.w > 0.0f) {
+            uint32_t x0, y0, x1, y1;
+            bounding_rect(texel.x, texel.y, texel.w, gx, grid_y(vc.height), x0, y0, x1, y1);
+            if (x1 > x0 && y1 > y0) {
+                w = x1 - x0;
+                h = y1 - y0;
+                t0 = vc.tile_base + y0 * gx + x0;
+            }
+        }
+    }
+    return ItemRect{t0, w | (gx << 16), w * h, gi};
+}
+
+// Writes the keys of a warp's 32 items, `total` in all, to output slots
+// base .. base + total - 1 (lane l's item from slot base + excl), in windows
+// of kKeyWindow slots, one coalesced store per lane and step (the owner-map
+// scheme above). Called by the whole warp.
+__device__ __forceinline__ void write_warp_keys(KeygenSmem& S, uint32_t warp, uint32_t lane, const ItemRect& it,
+                                                uint32_t excl, uint32_t total, uint32_t base, uint32_t capacity,
+                                                uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals) {
+    uint32_t* owner = S.owner[warp];
+    const uint32_t cnt = it.cnt;
+    S.t0[warp][lane] = it.t0;
+    S.wgx[warp][lane] = it.wgx;
+    S.excl[warp][lane] = excl;
+    S.gi[warp][lane] = it.gi;
+    for (uint32_t c0 = 0; c0 < total; c0 += kKeyWindow) {
+        const uint32_t span = min(kKeyWindow, total - c0);
+        // 1. owner map: segment starts, then a prefix max over the window
+        //    (owners grow with the slot; slot c0 belongs to the last lane
+        //    whose keys start at or before it)
+#pragma unroll
+        for (uint32_t q = 0; q < kKeyWindow / 32; ++q) owner[lane * (kKeyWindow / 32) + q] = 0;
+        __syncwarp();
+        if (cnt && excl >= c0 && excl < c0 + kKeyWindow) owner[excl - c0] = lane;
+        const uint32_t first_owner = 31u - __clz(__ballot_sync(0xFFFFFFFFu, excl <= c0 && cnt));
+        __syncwarp();
+        uint32_t run = 0, mine[kKeyWindow / 32];
+#pragma unroll
+        for (uint32_t q = 0; q < kKeyWindow / 32; ++q) {
+            run = max(run, owner[lane * (kKeyWindow / 32) + q]);
+            mine[q] = run;
+        }
+        uint32_t before = run;  // exclusive prefix max of the lanes' maxima
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, before, o);
+            if (lane >= o) before = max(before, x);
+        }
+        before = __shfl_up_sync(0xFFFFFFFFu, before, 1);
+        before = max(lane ? before : 0u, first_owner);
+        __syncwarp();
+#pragma unroll
+        for (uint32_t q = 0; q < kKeyWindow / 32; ++q) owner[lane * (kKeyWindow / 32) + q] = max(before, mine[q]);
+        __syncwarp();
+        // 2. slots lane, lane + 32, ...: one coalesced store group per step
+        for (uint32_t q = lane; q < span; q += 32u) {
+            if (uint64_t(base) + c0 + q < capacity) {
+                const uint32_t j = owner[q];
+                const uint32_t local = c0 + q - S.excl[warp][j];  // < 2^24: exact in a float
+                const uint32_t jwg = S.wgx[warp][j];
+                const uint32_t jw = jwg & 0xFFFFu;
+                // row = local / jw from a float quotient, corrected by one step
+                uint32_t ty = __float2uint_rz(__fdividef(float(local), float(jw)));
+                int32_t rem = int32_t(local) - int32_t(ty * jw);
+                if (rem < 0) {
+                    --ty;
+                    rem += int32_t(jw);
+                } else if (rem >= int32_t(jw)) {
+                    ++ty;
+                    rem -= int32_t(jw);
+                }
+                const uint32_t tile = S.t0[warp][j] + ty * (jwg >> 16) + uint32_t(rem);
+                const uint64_t pos = uint64_t(base) + c0 + q;
+                tiles[pos] = tile;
+                vals[pos] = S.gi[warp][j];
+            }
+        }
+        __syncwarp();  // the owner map is rebuilt for the next window
+    }
+    __syncwarp();  // the lane table is rewritten by the next items
+}
+
+// The depth-order tile-count scan fused with key duplication. Persistent
+// CTAs take partitions of kKeygenPart consecutive items in depth order by an
+// atomic ticket; warp w of a CTA owns the partition's items
+// [w kKeygenChunks 32, (w + 1) kKeygenChunks 32), in kKeygenChunks chunks of
+// 32 (one item per lane). Per partition:
+//  1. each lane gathers its items' splat texels and works out their tile
+//     rectangles, so its key counts;
+//  2. the counts are scanned across the warp, then across the CTA;
+//  3. one warp resolves the partition's exclusive prefix with the bounded
+//     decoupled look-back (prefix.slang:100-114 as restated in tpd_scan.cuh):
+//     the last partition's inclusive prefix is the frame's key count K;
+//  4. each lane writes its items' key offsets (the scan's output), and each
+//     warp writes its chunks' keys (write_warp_keys).
+// A key is stored as its tile id alone: the low 32 bits of the reference's
+// key are the depth, already in order (the items come in depth order), and
+// the depth of a key is that of its value's splat, so the sort needs only the
+// tile ids and the full keys can be rebuilt from (tile, value) when read.
+// Keys past the capacity are not written (the frame is flagged and rendered
+// again). The digit counts of the tile ids come from the preprocess, which
+// counts each Gaussian's tile rectangle row by row.
+// A CTA takes a ticket only when it starts on the partition, so every
+// partition a look-back waits on is being worked on by a running CTA and
+// publishes its aggregate soon.
+struct KeygenScanSmem {
+    KeygenSmem k;
+    uint32_t wtot[kKeygenWarps];  // key counts of the warps' items
+    uint32_t ticket;              // the partition being worked on
+    uint32_t excl;                // the partition's exclusive prefix
+};
+
 __global__ void __launch_bounds__(kKeygenThreads)
-    keygen_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
-                  const uint32_t* __restrict__ items_other, const uint32_t* __restrict__ offsets, uint32_t n_items,
-                  uint32_t n,
-                  const ViewConst* __restrict__ views, uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals,
-                  uint32_t capacity, uint32_t key_bits, uint32_t* __restrict__ ranges, uint32_t n_tiles,
-                  FrameCtl* ctl) {
-    __shared__ KeygenSmem S;
-    pdl_wait();     // launched as a dependent of the depth-order scan: its offsets are read below
+    keygen_scan_kernel(const Splat* __restrict__ splats, const uint32_t* __restrict__ items,
+                       const uint32_t* __restrict__ items_other, uint32_t n_items, uint32_t n,
+                       const ViewConst* __restrict__ views, uint32_t* __restrict__ offsets,
+                       uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals, uint32_t capacity,
+                       uint32_t* __restrict__ ranges, uint32_t n_tiles, uint64_t* desc, FrameCtl* ctl,
+                       uint32_t spin_limit, uint32_t never_publish) {
+    __shared__ KeygenScanSmem S;
+    pdl_wait();     // launched as a dependent of the depth sort's last pass: its order is read below
     pdl_trigger();  // the key sort's first counting kernel may be scheduled (it waits for this grid)
-    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-    const uint32_t warps_total = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->total_keys > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
-    if (ctl->status & kStatusFatal) return;
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
     const uint32_t count = min(ctl->depth_count, n_items);
     if (ctl->depth_skips & 1u) items = items_other;  // a skipped depth pass left the order there
     // ranges: (0xFFFFFFFF, 0) until the key sort's last pass narrows them
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x)
+    for (uint32_t t = blockIdx.x * blockDim.x + tid; t < n_tiles; t += gridDim.x * blockDim.x)
         reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0xFFFFFFFFu, 0u);
-    uint32_t* owner = S.owner[warp];
-    const uint32_t nwarps = (count + 31) / 32;
-
-    // The item index, key offset and splat texel (px, py, viewZ, radius) of a
-    // warp's next 32 items are loaded while it writes the keys of the current
-    // ones: the texel is a gather in depth order.
-    auto load_index = [&](uint32_t wi_, uint32_t& item, uint32_t& off) {
-        const uint32_t r = wi_ * 32u + lane;
-        item = 0xFFFFFFFFu;
-        off = 0;
-        if (wi_ < nwarps && r < count) {
-            item = items[r];
-            off = offsets[r];
+    const uint32_t nparts = (count + kKeygenPart - 1) / kKeygenPart;
+    const uint32_t tag = ctl->tag * 32u + kTagScan;
+    for (;;) {
+        // one thread reads the status for the whole CTA (a look-back of this
+        // grid may raise a fatal bit meanwhile, and every thread must take the
+        // same way through the barriers): a fatal status ends the CTA as a
+        // ticket past the last partition does
+        if (tid == 0)
+            S.ticket = (ctl->status & kStatusFatal) ? 0xFFFFFFFFu : atomicAdd(&ctl->ticket[kTicketScan], 1u);
+        __syncthreads();
+        const uint32_t part = S.ticket;
+        if (part >= nparts) break;  // (uniform)
+        const uint32_t r0 = part * kKeygenPart + warp * (kKeygenChunks * 32u) + lane;
+        uint32_t item[kKeygenChunks];
+        float4 texel[kKeygenChunks];
+#pragma unroll
+        for (uint32_t c = 0; c < kKeygenChunks; ++c) item[c] = r0 + 32u * c < count ? items[r0 + 32u * c] : 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t c = 0; c < kKeygenChunks; ++c)
+            texel[c] = item[c] < n_items ? reinterpret_cast<const float4*>(splats + item[c])[1]
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+        ItemRect rect[kKeygenChunks];
+        uint32_t incl[kKeygenChunks], ctot[kKeygenChunks], wtotal = 0, vis = 0;
+#pragma unroll
+        for (uint32_t c = 0; c < kKeygenChunks; ++c) {
+            rect[c] = item_rect(item[c], r0 + 32u * c < count, texel[c], n_items, n, views, ctl);
+            incl[c] = warp_inclusive_scan(rect[c].cnt);
+            ctot[c] = __shfl_sync(0xFFFFFFFFu, incl[c], 31);
+            wtotal += ctot[c];
+            vis += rect[c].cnt ? 1u : 0u;
         }
-    };
-    auto load_texel = [&](uint32_t item) {
-        return item < n_items ? reinterpret_cast<const float4*>(splats + item)[1] : make_float4(0.f, 0.f, 0.f, 0.f);
-    };
-    uint32_t item_c, off_c;
-    load_index(warp_global, item_c, off_c);
-    float4 texel_c = load_texel(item_c);
-
-    for (uint32_t wi = warp_global; wi < nwarps; wi += warps_total) {
-        uint32_t item_n, off_n;
-        load_index(wi + warps_total, item_n, off_n);
-        const uint32_t r = wi * 32u + lane;
-        // per item: first tile (row-major in its view), rect width and height, view grid width
-        uint32_t w = 1, h = 0, gx = 1, off = 0, gi = 0, t0 = 0;
-        if (r < count) {
-            const uint32_t item = item_c;
-            off = off_c;
-            if (TPD_INBOUNDS(ctl, 21, item, n_items)) {
-                const uint32_t v = n_items == n ? 0u : item / n;  // one view: no division
-                gi = item - v * n;
-                const ViewConst& vc = views[v];
-                gx = grid_x(vc.width);
-                const float4 texel = texel_c;
-                if (texel.w > 0.0f) {
-                    uint32_t x0, y0, x1, y1;
-                    bounding_rect(texel.x, texel.y, texel.w, gx, grid_y(vc.height), x0, y0, x1, y1);
-                    if (x1 > x0 && y1 > y0) {
-                        w = x1 - x0;
-                        h = y1 - y0;
-                        t0 = vc.tile_base + y0 * gx + x0;
-                    }
+        vis = warp_sum(vis);
+        if (lane == 0) {
+            S.wtot[warp] = wtotal;
+            if (vis) atomicAdd(&ctl->visible, vis);
+        }
+        __syncthreads();
+        uint32_t wbase = 0, total = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kKeygenWarps; ++w) {
+            const uint32_t sw = S.wtot[w];
+            wbase += w < warp ? sw : 0u;
+            total += sw;
+        }
+        if (warp == 0) {
+            const uint32_t ex = warp_lookback(desc, part, total, tag, &ctl->status, spin_limit, never_publish != 0);
+            if (lane == 0) {
+                S.excl = ex;
+                if (part == nparts - 1u) {
+                    ctl->total_keys = ex + total;
+                    if (ex + total > capacity) atomicOr(&ctl->status, kStatusKeyOverflow);
                 }
             }
         }
-        const uint32_t cnt = w * h;
-        const uint32_t incl = warp_inclusive_scan(cnt);
-        const uint32_t excl = incl - cnt;
-        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        const uint32_t base = __shfl_sync(0xFFFFFFFFu, off, 0);
-        S.t0[warp][lane] = t0;
-        S.wgx[warp][lane] = w | (gx << 16);
-        S.excl[warp][lane] = excl;
-        S.gi[warp][lane] = gi;
-        const float4 texel_n = load_texel(item_n);
-
-        for (uint32_t c0 = 0; c0 < total; c0 += kKeyWindow) {
-            const uint32_t span = min(kKeyWindow, total - c0);
-            // 1. owner map: segment starts, then a prefix max over the window
-            //    (owners grow with the slot; slot c0 belongs to the last lane
-            //    whose keys start at or before it)
+        __syncthreads();
+        uint32_t base = S.excl + wbase;
 #pragma unroll
-            for (uint32_t q = 0; q < kKeyWindow / 32; ++q) owner[lane * (kKeyWindow / 32) + q] = 0;
-            __syncwarp();
-            if (cnt && excl >= c0 && excl < c0 + kKeyWindow) owner[excl - c0] = lane;
-            const uint32_t first_owner = 31u - __clz(__ballot_sync(0xFFFFFFFFu, excl <= c0 && cnt));
-            __syncwarp();
-            uint32_t run = 0, mine[kKeyWindow / 32];
-#pragma unroll
-            for (uint32_t q = 0; q < kKeyWindow / 32; ++q) {
-                run = max(run, owner[lane * (kKeyWindow / 32) + q]);
-                mine[q] = run;
-            }
-            uint32_t before = run;  // exclusive prefix max of the lanes' maxima
-#pragma unroll
-            for (uint32_t o = 1; o < 32; o <<= 1) {
-                const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, before, o);
-                if (lane >= o) before = max(before, x);
-            }
-            before = __shfl_up_sync(0xFFFFFFFFu, before, 1);
-            before = max(lane ? before : 0u, first_owner);
-            __syncwarp();
-#pragma unroll
-            for (uint32_t q = 0; q < kKeyWindow / 32; ++q) owner[lane * (kKeyWindow / 32) + q] = max(before, mine[q]);
-            __syncwarp();
-            // 2. slots lane, lane + 32, ...: one coalesced store group per step
-            for (uint32_t q = lane; q < span; q += 32u) {
-                if (uint64_t(base) + c0 + q < capacity) {
-                    const uint32_t j = owner[q];
-                    const uint32_t local = c0 + q - S.excl[warp][j];  // < 2^24: exact in a float
-                    const uint32_t jwg = S.wgx[warp][j];
-                    const uint32_t jw = jwg & 0xFFFFu;
-                    // row = local / jw from a float quotient, corrected by one step
-                    uint32_t ty = __float2uint_rz(__fdividef(float(local), float(jw)));
-                    int32_t rem = int32_t(local) - int32_t(ty * jw);
-                    if (rem < 0) {
-                        --ty;
-                        rem += int32_t(jw);
-                    } else if (rem >= int32_t(jw)) {
-                        ++ty;
-                        rem -= int32_t(jw);
-                    }
-                    const uint32_t tile = S.t0[warp][j] + ty * (jwg >> 16) + uint32_t(rem);
-                    const uint64_t pos = uint64_t(base) + c0 + q;
-                    tiles[pos] = tile;
-                    vals[pos] = S.gi[warp][j];
-                }
-            }
-            __syncwarp();  // the owner map is rebuilt for the next window
+        for (uint32_t c = 0; c < kKeygenChunks; ++c) {
+            const uint32_t excl = incl[c] - rect[c].cnt;
+            if (r0 + 32u * c < count) offsets[r0 + 32u * c] = base + excl;
+            write_warp_keys(S.k, warp, lane, rect[c], excl, ctot[c], base, capacity, tiles, vals);
+            base += ctot[c];
         }
-        __syncwarp();  // the lane table is rewritten by the next items
-        item_c = item_n;
-        off_c = off_n;
-        texel_c = texel_n;
+        __syncthreads();  // S.ticket, S.wtot and S.excl are rewritten for the next partition
     }
 }
 
 int keygen_setup() {
     int r = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, keygen_kernel, kKeygenThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, keygen_scan_kernel, kKeygenThreads, 0);
     return r > 0 ? r : 1;
 }
 
 }  // namespace
 
-void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* items_other, const uint32_t* offsets,
-                   uint32_t n_items, uint32_t n,
-                   const ViewConst* views, uint32_t* tiles, uint32_t* vals, uint32_t capacity, uint32_t key_bits,
-                   uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl, int num_sms, cudaStream_t s) {
+void launch_keygen_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t n_items,
+                        uint32_t n, const ViewConst* views, uint32_t* offsets, uint32_t* tiles, uint32_t* vals,
+                        uint32_t capacity, uint32_t* ranges, uint32_t n_tiles, uint64_t* desc, FrameCtl* ctl,
+                        uint32_t spin_limit, uint32_t never_publish, int num_sms, cudaStream_t s) {
     if (n_items == 0 || n == 0) return;
-    const uint64_t warps = (uint64_t(n_items) + 31) / 32;
-    uint64_t blocks = (warps * 32 + kKeygenThreads - 1) / kKeygenThreads;
-    const int per_sm = device_once(keygen_setup);  // resident CTAs per SM (shared memory bound)
+    const uint64_t parts = (uint64_t(n_items) + kKeygenPart - 1) / kKeygenPart;
+    const int per_sm = device_once(keygen_setup);  // resident CTAs per SM
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
-    blocks = blocks < cap ? blocks : cap;
-    launch_dependent(keygen_kernel, dim3(unsigned(blocks)), dim3(kKeygenThreads), 0, s, splats, items, items_other,
-                     offsets, n_items, n, views, tiles, vals, capacity, key_bits, ranges, n_tiles, ctl);
+    const uint64_t blocks = parts < cap ? parts : cap;
+    launch_dependent(keygen_scan_kernel, dim3(unsigned(blocks)), dim3(kKeygenThreads), 0, s, splats, items,
+                     items_other, n_items, n, views, offsets, tiles, vals, capacity, ranges, n_tiles, desc, ctl,
+                     spin_limit, never_publish);
 }
 
 namespace {

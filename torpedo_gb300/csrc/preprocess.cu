@@ -16,11 +16,11 @@
 // depth-sort key (view << 32 | bits(viewZ)) whose digit histograms are
 // accumulated here, and the digits of the tile ids its keys will carry are
 // counted from its tile rectangle for the key sort (count_tile_row). The tile
-// counts are scanned afterwards in depth order
-// (scan_tiles_kernel<true>: gather + decoupled look-back, partitions by atomic
-// ticket). Arithmetic follows the shader source left to right with matrix
-// products accumulated k = 0..n-1; this file is compiled with --fmad=false so
-// no product is fused into an add.
+// counts are scanned afterwards in depth order, inside keygen.cu's fused scan
+// and key duplication (scan_tiles_kernel is the standalone scan). Arithmetic
+// follows the shader source left to right with matrix products accumulated
+// k = 0..n-1; this file is compiled with --fmad=false so no product is fused
+// into an add.
 #include <algorithm>
 
 #include "tpd_common.cuh"
@@ -439,58 +439,29 @@ __global__ void __launch_bounds__(kPreThreads, 3) preprocess_kernel(PreprocessAr
             if (S.hist[p][d]) atomicAdd(&a.ctl->depth_hist[p][d], S.hist[p][d]);
 }
 
-// Exclusive scan of tile counts over partitions of 256 threads x 4 items
-// (prefix.slang:40-158); kGather: counts of splats[items[r]] (depth order),
-// else of splats[r]. Total -> ctl->total_keys, non-empty count -> ctl->visible.
+// Exclusive scan of Splat.tiles over partitions of 256 threads x 4 items
+// (prefix.slang:40-158), partitions taken by atomic ticket. Total ->
+// ctl->total_keys, non-empty count -> ctl->visible. (The frame scans its
+// counts in depth order inside keygen_scan_kernel.)
 constexpr uint32_t kScanThreads = 256;
+constexpr uint32_t kScanItems = 4;
 
-// kItems consecutive items per thread: 4 for the standalone scan, 16 for the
-// depth-order scan of the frame (4096-item partitions: a quarter of the
-// look-back chain; the item indices are read 16 bytes at a time). The
-// depth-order scan covers the ctl->depth_count items the depth sort kept
-// (at most n): the grid is sized for n and the partitions past the count exit.
-template <bool kGather, uint32_t kItems>
 __global__ void __launch_bounds__(kScanThreads)
-    scan_tiles_kernel(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t n_max,
-                      uint32_t* offsets, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish) {
-    constexpr uint32_t kScanTile = kScanThreads * kItems;
+    scan_tiles_kernel(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
+                      uint32_t spin_limit, uint32_t never_publish) {
+    constexpr uint32_t kScanTile = kScanThreads * kScanItems;
     __shared__ uint32_t s_part, s_excl;
-    // launched as a dependent of the stream's previous kernel: its output is
-    // read below. No early trigger: the next kernel is one wave of CTAs, which
-    // must be placed on empty SMs, not onto the first ones this grid frees
-    pdl_wait();
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t n = kGather ? min(ctl->depth_count, n_max) : n_max;
-    if (kGather && (ctl->depth_skips & 1u)) items = items_other;  // a skipped depth pass left the order there
     if (tid == 0) s_part = atomicAdd(&ctl->ticket[kTicketScan], 1u);
     __syncthreads();
     const uint32_t part = s_part;
     if (part * kScanTile >= n) return;  // (uniform) past the items; nothing waits on it
-    const uint32_t base = part * kScanTile + tid * kItems;
-    uint32_t it[kItems];
-    if constexpr (kGather && kItems % 4 == 0) {
+    const uint32_t base = part * kScanTile + tid * kScanItems;
+    uint32_t v[kScanItems], sum = 0, vis = 0;
 #pragma unroll
-        for (uint32_t k = 0; k < kItems; k += 4) {
-            if (base + k + 3 < n) {
-                const uint4 q = *reinterpret_cast<const uint4*>(items + base + k);
-                it[k] = q.x;
-                it[k + 1] = q.y;
-                it[k + 2] = q.z;
-                it[k + 3] = q.w;
-            } else {
-#pragma unroll
-                for (uint32_t j = 0; j < 4; ++j) it[k + j] = base + k + j < n ? items[base + k + j] : 0u;
-            }
-        }
-    } else {
-#pragma unroll
-        for (uint32_t k = 0; k < kItems; ++k) it[k] = kGather ? (base + k < n ? items[base + k] : 0u) : base + k;
-    }
-    uint32_t v[kItems], sum = 0, vis = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < kItems; ++k) {
-        v[k] = base + k < n ? splats[it[k]].tiles : 0u;
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? splats[base + k].tiles : 0u;
         sum += v[k];
         vis += v[k] ? 1u : 0u;
     }
@@ -518,7 +489,7 @@ __global__ void __launch_bounds__(kScanThreads)
     __syncthreads();
     uint32_t run = s_excl + wbase + incl - sum;
 #pragma unroll
-    for (uint32_t k = 0; k < kItems; ++k) {
+    for (uint32_t k = 0; k < kScanItems; ++k) {
         if (base + k < n) offsets[base + k] = run;
         run += v[k];
     }
@@ -570,18 +541,8 @@ void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s) {
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
                        uint32_t spin_limit, uint32_t never_publish, cudaStream_t s) {
     if (n == 0) return;
-    const uint32_t blocks = (n + kScanThreads * 4 - 1) / (kScanThreads * 4);
-    scan_tiles_kernel<false, 4><<<blocks, kScanThreads, 0, s>>>(splats, nullptr, nullptr, n, offsets, desc, ctl,
-                                                                spin_limit, never_publish);
-}
-
-void launch_depth_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t max_count,
-                       uint32_t* offsets, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish,
-                       cudaStream_t s) {
-    if (max_count == 0) return;
-    const uint32_t blocks = (max_count + kScanThreads * 16 - 1) / (kScanThreads * 16);
-    launch_dependent(scan_tiles_kernel<true, 16>, dim3(blocks), dim3(kScanThreads), 0, s, splats, items, items_other,
-                     max_count, offsets, desc, ctl, spin_limit, never_publish);
+    const uint32_t blocks = (n + kScanThreads * kScanItems - 1) / (kScanThreads * kScanItems);
+    scan_tiles_kernel<<<blocks, kScanThreads, 0, s>>>(splats, n, offsets, desc, ctl, spin_limit, never_publish);
 }
 
 void launch_pack_records(const float* means, const float* log_scales, const float* quats, const float* logits,

@@ -82,33 +82,32 @@ void launch_frame_begin(FrameCtl* ctl, const float* transforms, uint32_t n_ent, 
                         uint32_t n_views, float* ent_mats, cudaStream_t s);
 void launch_preprocess(const PreprocessArgs& a, int num_sms, cudaStream_t s);
 
-// Tile counts of the ctl->depth_count (view, Gaussian) items in depth order
-// (at most max_count), gathered through items[r] = v * n + i, scanned into
-// exclusive key offsets offsets[r]; the total goes to ctl->total_keys and the
-// non-empty count to ctl->visible.
-// items: where the depth sort leaves the order with no pass skipped;
-// items_other: the other buffer, which holds it when ctl->depth_skips is odd.
-void launch_depth_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t max_count,
-                       uint32_t* offsets, uint64_t* desc, FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish,
-                       cudaStream_t s);
-
 // Standalone exclusive scan of Splat.tiles (prefix.slang); total -> ctl->total_keys.
 void launch_scan_tiles(const Splat* splats, uint32_t n, uint32_t* offsets, uint64_t* desc, FrameCtl* ctl,
                        uint32_t spin_limit, uint32_t never_publish, cudaStream_t s);
 
-// keygen.slang's keys (tile_base + tile) << 32 | bits(viewZ) and vals = Gaussian
-// index, for the items[] in depth order with their key offsets. The items come
-// in depth order, so only the tile id of each key is written (tiles[], u32):
-// the depth half of a key is the depth of its value's splat
-// (launch_materialize_keys). K is read from ctl->total_keys; keys beyond
-// capacity are dropped and flag the frame (kStatusKeyOverflow). Also presets
-// ranges (2 x n_tiles u32) to (0xFFFFFFFF, 0) for the key sort's last pass.
-// The digit counts of the tile ids come from the preprocess (tile_bits).
-// items[0 .. ctl->depth_count) index the n_items = n_views x n splats.
-void launch_keygen(const Splat* splats, const uint32_t* items, const uint32_t* items_other, const uint32_t* offsets,
-                   uint32_t n_items, uint32_t n, const ViewConst* views, uint32_t* tiles, uint32_t* vals,
-                   uint32_t capacity, uint32_t key_bits, uint32_t* ranges, uint32_t n_tiles, FrameCtl* ctl,
-                   int num_sms, cudaStream_t s);
+// Items (view, Gaussian) in depth order per partition of the fused scan and
+// key duplication: its look-back descriptors number n_items / kKeygenPart + 2.
+constexpr uint32_t kKeygenPart = 512;
+
+// The tile counts of the ctl->depth_count (view, Gaussian) items in depth
+// order (items[r] = v * n + i < n_items) scanned into exclusive key offsets
+// offsets[r] (prefix.slang), fused with keygen.slang's key duplication: keys
+// (tile_base + tile) << 32 | bits(viewZ) with vals = Gaussian index. The
+// items come in depth order, so only the tile id of each key is written
+// (tiles[], u32): the depth half of a key is the depth of its value's splat
+// (launch_materialize_keys). K goes to ctl->total_keys and the non-empty
+// count to ctl->visible; keys beyond capacity are dropped and flag the frame
+// (kStatusKeyOverflow). Also presets ranges (2 x n_tiles u32) to
+// (0xFFFFFFFF, 0) for the key sort's last pass. The digit counts of the tile
+// ids come from the preprocess (tile_bits).
+// items: where the depth sort leaves the order with no pass skipped;
+// items_other: the other buffer, which holds it when ctl->depth_skips is odd.
+// desc: look-back descriptors (tag ctl->tag * 32 + kTagScan), never cleared.
+void launch_keygen_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t n_items,
+                        uint32_t n, const ViewConst* views, uint32_t* offsets, uint32_t* tiles, uint32_t* vals,
+                        uint32_t capacity, uint32_t* ranges, uint32_t n_tiles, uint64_t* desc, FrameCtl* ctl,
+                        uint32_t spin_limit, uint32_t never_publish, int num_sms, cudaStream_t s);
 
 // keys[i] = tiles[i] << 32 | bits(viewZ of splat vals[i] in the tile's view),
 // i < min(ctl->total_keys, capacity): the 64-bit (tile | depth) keys of a
