@@ -406,6 +406,12 @@ void enqueue_frame(tpd_engine* e, bool io = true, bool state = true, uint32_t* r
     pa.depth_key_bits = e->depth_key_bits;
     pa.tile_bits = e->key_bits - 32;  // the key sort's digit counts
     pa.ctl = e->d_ctl;
+    // counted key-sort passes (default): keygen counts the first pass's
+    // partition rows, which the preprocess clears
+    const bool counted = e->settings.key_sort_lookback == 0;
+    const uint32_t key_parts = std::max(1u, uint32_t((e->capacity + 4095u) / 4096u));
+    pa.zero_words = counted ? e->d_sort_work : nullptr;
+    pa.zero_count = counted ? uint64_t(key_parts) * 256u : 0u;
     launch_preprocess(pa, e->num_sms, s);
     mark(1);
     const uint32_t spin = e->settings.spin_limit ? e->settings.spin_limit : kDefaultSpin;
@@ -430,8 +436,9 @@ void enqueue_frame(tpd_engine* e, bool io = true, bool state = true, uint32_t* r
     mark(2);
     const uint32_t cap = uint32_t(e->capacity);
     launch_keygen_scan(e->d_splats, order, order_other, items, e->n, e->d_views, e->d_offsets, e->d_tiles[0],
-                       e->d_vals[0], cap, e->d_ranges, e->total_tiles, e->d_desc_pre, e->d_ctl, spin,
-                       e->settings.test_never_publish, e->num_sms, s);
+                       e->d_vals[0], cap, e->d_ranges, e->total_tiles, e->d_desc_pre,
+                       counted ? e->d_sort_work : nullptr, e->d_ctl, spin, e->settings.test_never_publish, e->num_sms,
+                       s);
     mark(3);
     SortPlan kp;
     kp.first_bit = 0;  // tile ids; the depth half of the keys is already in order
@@ -446,8 +453,9 @@ void enqueue_frame(tpd_engine* e, bool io = true, bool state = true, uint32_t* r
     kp.ranges = e->d_ranges;  // the last pass writes the tile ranges
     kp.n_tiles = e->total_tiles;
     // counted passes (default), or onesweep passes with a look-back
-    if (e->settings.key_sort_lookback == 0) {
+    if (counted) {
         kp.counted_work = e->d_sort_work;
+        kp.precounted = true;  // keygen counted the first pass's rows
         kp.ctas_per_sm = e->settings.sort_ctas_per_sm == 2 ? 2 : 3;
     }
     e->sorted_in_alt = launch_sort(e->d_tiles[0], e->d_vals[0], e->d_tiles[1], e->d_vals[1], cap, kp, e->d_desc_sort,

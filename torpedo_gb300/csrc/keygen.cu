@@ -25,6 +25,7 @@ namespace {
 constexpr uint32_t kKeygenThreads = 256;
 constexpr uint32_t kKeygenChunks = kKeygenPart / kKeygenThreads;  // 32-item chunks per warp and partition
 static_assert(kKeygenChunks * kKeygenThreads == kKeygenPart, "a partition is whole chunks of every warp");
+static_assert(kKeygenThreads == 256, "a thread per low tile-id digit flushes the partition counts");
 
 // A warp writes the keys of 32 consecutive items (one per lane), whose keys
 // are contiguous, in windows of kKeyWindow output slots:
@@ -76,9 +77,16 @@ __device__ __forceinline__ ItemRect item_rect(uint32_t item, bool valid, float4 
 // base .. base + total - 1 (lane l's item from slot base + excl), in windows
 // of kKeyWindow slots, one coalesced store per lane and step (the owner-map
 // scheme above). Called by the whole warp.
+// With count_rows, each written key also adds one to its 4096-key sort
+// partition's count of its low tile-id digit: in s_cnt (kCountWindow rows,
+// partitions p0 .. p0 + kCountWindow - 1) when its partition is there, else
+// straight into count_rows.
+constexpr uint32_t kCountWindow = 8;
+
 __device__ __forceinline__ void write_warp_keys(KeygenSmem& S, uint32_t warp, uint32_t lane, const ItemRect& it,
                                                 uint32_t excl, uint32_t total, uint32_t base, uint32_t capacity,
-                                                uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals) {
+                                                uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals,
+                                                uint32_t* s_cnt, uint32_t p0, uint32_t* __restrict__ count_rows) {
     uint32_t* owner = S.owner[warp];
     const uint32_t cnt = it.cnt;
     S.t0[warp][lane] = it.t0;
@@ -135,6 +143,13 @@ __device__ __forceinline__ void write_warp_keys(KeygenSmem& S, uint32_t warp, ui
                 const uint64_t pos = uint64_t(base) + c0 + q;
                 tiles[pos] = tile;
                 vals[pos] = S.gi[warp][j];
+                if (count_rows) {
+                    const uint32_t part = uint32_t(pos >> 12), d = tile & 255u;
+                    if (part - p0 < kCountWindow)
+                        atomicAdd(&s_cnt[(part - p0) * 256u + d], 1u);
+                    else
+                        atomicAdd(&count_rows[size_t(part) * 256u + d], 1u);
+                }
             }
         }
         __syncwarp();  // the owner map is rebuilt for the next window
@@ -164,9 +179,14 @@ __device__ __forceinline__ void write_warp_keys(KeygenSmem& S, uint32_t warp, ui
 // counts each Gaussian's tile rectangle row by row.
 // A CTA takes a ticket only when it starts on the partition, so every
 // partition a look-back waits on is being worked on by a running CTA and
-// publishes its aggregate soon.
+// publishes its aggregate soon. With count_rows, a partition's keys (one
+// contiguous run of slots) are also counted per 4096-key sort partition and
+// low tile-id digit in shared memory, and the non-zero counts added into
+// count_rows with one atomic each once the partition is written: the key
+// sort's first pass then needs no counting kernel.
 struct KeygenScanSmem {
     KeygenSmem k;
+    uint32_t cnt[kCountWindow * 256];  // low-digit counts of sort partitions p0 .. p0 + kCountWindow - 1
     uint32_t wtot[kKeygenWarps];  // key counts of the warps' items
     uint32_t ticket;              // the partition being worked on
     uint32_t excl;                // the partition's exclusive prefix
@@ -177,8 +197,9 @@ __global__ void __launch_bounds__(kKeygenThreads)
                        const uint32_t* __restrict__ items_other, uint32_t n_items, uint32_t n,
                        const ViewConst* __restrict__ views, uint32_t* __restrict__ offsets,
                        uint32_t* __restrict__ tiles, uint32_t* __restrict__ vals, uint32_t capacity,
-                       uint32_t* __restrict__ ranges, uint32_t n_tiles, uint64_t* desc, FrameCtl* ctl,
-                       uint32_t spin_limit, uint32_t never_publish) {
+                       uint32_t* __restrict__ ranges, uint32_t n_tiles, uint64_t* desc,
+                       uint32_t* __restrict__ count_rows, FrameCtl* ctl, uint32_t spin_limit,
+                       uint32_t never_publish) {
     __shared__ KeygenScanSmem S;
     pdl_wait();     // launched as a dependent of the depth sort's last pass: its order is read below
     pdl_trigger();  // the key sort's first counting kernel may be scheduled (it waits for this grid)
@@ -190,6 +211,8 @@ __global__ void __launch_bounds__(kKeygenThreads)
         reinterpret_cast<uint2*>(ranges)[t] = make_uint2(0xFFFFFFFFu, 0u);
     const uint32_t nparts = (count + kKeygenPart - 1) / kKeygenPart;
     const uint32_t tag = ctl->tag * 32u + kTagScan;
+#pragma unroll
+    for (uint32_t w = 0; w < kCountWindow; ++w) S.cnt[w * 256u + tid] = 0;  // (before the first barrier)
     for (;;) {
         // one thread reads the status for the whole CTA (a look-back of this
         // grid may raise a fatal bit meanwhile, and every thread must take the
@@ -243,15 +266,29 @@ __global__ void __launch_bounds__(kKeygenThreads)
             }
         }
         __syncthreads();
+        const uint32_t p0 = S.excl >> 12;  // the sort partition of the partition's first key
         uint32_t base = S.excl + wbase;
 #pragma unroll
         for (uint32_t c = 0; c < kKeygenChunks; ++c) {
             const uint32_t excl = incl[c] - rect[c].cnt;
             if (r0 + 32u * c < count) offsets[r0 + 32u * c] = base + excl;
-            write_warp_keys(S.k, warp, lane, rect[c], excl, ctot[c], base, capacity, tiles, vals);
+            write_warp_keys(S.k, warp, lane, rect[c], excl, ctot[c], base, capacity, tiles, vals, S.cnt, p0,
+                            count_rows);
             base += ctot[c];
         }
-        __syncthreads();  // S.ticket, S.wtot and S.excl are rewritten for the next partition
+        __syncthreads();  // S.ticket, S.wtot and S.excl are rewritten for the next partition; S.cnt is complete
+        if (count_rows) {
+            // thread d flushes and clears digit d's counts (the next
+            // partition's keys add to them only after its barriers)
+#pragma unroll
+            for (uint32_t w = 0; w < kCountWindow; ++w) {
+                const uint32_t c = S.cnt[w * 256u + tid];
+                if (c) {
+                    atomicAdd(&count_rows[size_t(p0 + w) * 256u + tid], c);
+                    S.cnt[w * 256u + tid] = 0;
+                }
+            }
+        }
     }
 }
 
@@ -265,16 +302,16 @@ int keygen_setup() {
 
 void launch_keygen_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t n_items,
                         uint32_t n, const ViewConst* views, uint32_t* offsets, uint32_t* tiles, uint32_t* vals,
-                        uint32_t capacity, uint32_t* ranges, uint32_t n_tiles, uint64_t* desc, FrameCtl* ctl,
-                        uint32_t spin_limit, uint32_t never_publish, int num_sms, cudaStream_t s) {
+                        uint32_t capacity, uint32_t* ranges, uint32_t n_tiles, uint64_t* desc, uint32_t* count_rows,
+                        FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, int num_sms, cudaStream_t s) {
     if (n_items == 0 || n == 0) return;
     const uint64_t parts = (uint64_t(n_items) + kKeygenPart - 1) / kKeygenPart;
     const int per_sm = device_once(keygen_setup);  // resident CTAs per SM
     const uint64_t cap = uint64_t(num_sms > 0 ? num_sms : 148) * uint64_t(per_sm);  // persistent
     const uint64_t blocks = parts < cap ? parts : cap;
     launch_dependent(keygen_scan_kernel, dim3(unsigned(blocks)), dim3(kKeygenThreads), 0, s, splats, items,
-                     items_other, n_items, n, views, offsets, tiles, vals, capacity, ranges, n_tiles, desc, ctl,
-                     spin_limit, never_publish);
+                     items_other, n_items, n, views, offsets, tiles, vals, capacity, ranges, n_tiles, desc,
+                     count_rows, ctl, spin_limit, never_publish);
 }
 
 namespace {

@@ -328,6 +328,14 @@ __global__ void __launch_bounds__(kPreThreads, 3) preprocess_kernel(PreprocessAr
     };
     if (blockIdx.x < nchunks) issue(blockIdx.x, 0);
     cp_async_commit();
+    // (while the first records arrive) the words to clear: the key sort's
+    // precounted rows, which keygen adds its digit counts into
+    if (a.zero_words) {
+        uint4* z = reinterpret_cast<uint4*>(a.zero_words);
+        const uint64_t n4 = a.zero_count / 4u;
+        for (uint64_t k = uint64_t(blockIdx.x) * kPreThreads + tid; k < n4; k += uint64_t(gridDim.x) * kPreThreads)
+            z[k] = make_uint4(0u, 0u, 0u, 0u);
+    }
 
     uint32_t it = 0;
     for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, ++it) {

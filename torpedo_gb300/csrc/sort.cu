@@ -505,6 +505,42 @@ __host__ __device__ inline size_t counted_work_words(uint32_t parts) {
 
 __device__ __forceinline__ uint32_t ld_cg_u32(const uint32_t* p) { return __ldcg(p); }
 
+// Rows of the chunk's partitions [first, first + csize) -> offsets within the
+// chunk, in place, and the chunk's total per digit into chunk_rows (thread =
+// digit; the rows are loaded together, then scanned).
+__device__ __forceinline__ void scan_chunk_rows(uint32_t* rows, uint32_t* chunk_rows, uint32_t chunk, uint32_t first,
+                                                uint32_t csize, uint32_t tid) {
+    uint32_t c[kChunkParts];
+#pragma unroll
+    for (uint32_t q = 0; q < kChunkParts; ++q)
+        c[q] = q < csize ? ld_cg_u32(rows + size_t(first + q) * 256 + tid) : 0u;
+    uint32_t run = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < kChunkParts; ++q) {
+        if (q < csize) rows[size_t(first + q) * 256 + tid] = run;
+        run += c[q];
+    }
+    chunk_rows[size_t(chunk) * 256 + tid] = run;
+}
+
+// The last chunk: each chunk's total -> its base, from the pass's global digit
+// offsets (the exclusive scan of hist_digit over digits). Called by the whole CTA.
+__device__ __forceinline__ void scan_chunk_bases(uint32_t* chunk_rows, uint32_t nchunks, uint32_t hist_digit,
+                                                 uint32_t* wsum, uint32_t tid) {
+    uint32_t gbase = block_exclusive_scan256<8>(hist_digit, wsum);
+    uint32_t c[kChunkParts];
+    for (uint32_t c0 = 0; c0 < nchunks; c0 += kChunkParts) {  // chunk totals, kChunkParts at a time
+#pragma unroll
+        for (uint32_t q = 0; q < kChunkParts; ++q)
+            c[q] = c0 + q < nchunks ? ld_cg_u32(chunk_rows + size_t(c0 + q) * 256 + tid) : 0u;
+#pragma unroll
+        for (uint32_t q = 0; q < kChunkParts; ++q) {
+            if (c0 + q < nchunks) chunk_rows[size_t(c0 + q) * 256 + tid] = gbase;
+            gbase += c[q];
+        }
+    }
+}
+
 template <int kItems, typename KeyT>
 __global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __restrict__ keys, uint32_t capacity,
                                                               uint32_t pass, uint32_t shift, uint32_t bits,
@@ -575,18 +611,7 @@ __global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __rest
     __syncthreads();
     if (!last) return;
     // the chunk's last CTA: offsets within the chunk, in place, and its total
-    // (the chunk's rows are loaded together, then scanned)
-    uint32_t c[kChunkParts];
-#pragma unroll
-    for (uint32_t q = 0; q < kChunkParts; ++q)
-        c[q] = q < csize ? ld_cg_u32(rows + size_t(first + q) * 256 + tid) : 0u;
-    uint32_t run = 0;
-#pragma unroll
-    for (uint32_t q = 0; q < kChunkParts; ++q) {
-        if (q < csize) rows[size_t(first + q) * 256 + tid] = run;
-        run += c[q];
-    }
-    chunk_rows[size_t(chunk) * 256 + tid] = run;
+    scan_chunk_rows(rows, chunk_rows, chunk, first, csize, tid);
     __syncthreads();
     if (tid == 0) {
         arrivals[chunk] = 0;
@@ -597,18 +622,48 @@ __global__ void __launch_bounds__(256) partition_count_kernel(const KeyT* __rest
     __syncthreads();
     if (!last) return;
     // the last chunk: each chunk's base, from the pass's global digit offsets
-    const uint32_t hd = TPD_INBOUNDS(ctl, 19, pass, 8) ? hist[pass][tid] : 0u;
-    uint32_t gbase = block_exclusive_scan256<8>(hd, wsum);
-    for (uint32_t c0 = 0; c0 < nchunks; c0 += kChunkParts) {  // chunk totals, kChunkParts at a time
-#pragma unroll
-        for (uint32_t q = 0; q < kChunkParts; ++q)
-            c[q] = c0 + q < nchunks ? ld_cg_u32(chunk_rows + size_t(c0 + q) * 256 + tid) : 0u;
-#pragma unroll
-        for (uint32_t q = 0; q < kChunkParts; ++q) {
-            if (c0 + q < nchunks) chunk_rows[size_t(c0 + q) * 256 + tid] = gbase;
-            gbase += c[q];
-        }
+    scan_chunk_bases(chunk_rows, nchunks, TPD_INBOUNDS(ctl, 19, pass, 8) ? hist[pass][tid] : 0u, wsum, tid);
+    if (tid == 0) arrivals[counted_chunks(max_parts)] = 0;
+}
+
+// The first pass of a sort whose partition rows were counted by the kernel
+// that wrote the keys (keygen_scan_kernel adds each partition's digit counts
+// into rows[] with atomics, on rows that were zero): no keys are read. One
+// CTA per chunk of kChunkParts partitions scans its rows in place and writes
+// the chunk's totals; the last chunk to finish (an arrival count, reset by
+// it) scans the chunk totals into chunk bases, as partition_count_kernel's
+// last arrivers do.
+__global__ void __launch_bounds__(256) chunk_scan_kernel(uint32_t capacity, uint32_t pass,
+                                                         const uint32_t (*hist)[256], uint32_t fixed_count,
+                                                         uint32_t max_parts, uint32_t* __restrict__ work,
+                                                         FrameCtl* ctl, uint32_t abort_mask) {
+    __shared__ uint32_t wsum[8];
+    __shared__ bool last;
+    const uint32_t tid = threadIdx.x;
+    pdl_wait();     // the rows come from the kernel before this one
+    pdl_trigger();  // the scatter may be scheduled; it waits for this grid
+    const uint32_t K = (ctl->status & abort_mask) ? 0u : min(fixed_count ? fixed_count : ctl->total_keys, capacity);
+    const uint32_t nparts = min((K + 4095u) / 4096u, max_parts);
+    const uint32_t nchunks = uint32_t(counted_chunks(nparts));
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= nchunks) return;  // (uniform)
+    uint32_t* rows = work;
+    uint32_t* chunk_rows = work + 256 * size_t(max_parts);
+    uint32_t* arrivals = chunk_rows + 256 * counted_chunks(max_parts);
+    const uint32_t first = chunk * kChunkParts, csize = min(kChunkParts, nparts - first);
+    scan_chunk_rows(rows, chunk_rows, chunk, first, csize, tid);
+    // the chunk totals are visible device-wide before the arrival is counted
+    // (barrier, then thread 0's cumulative fence); the last arriver's fence
+    // after its count orders its reads after every chunk's totals
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        last = atomicAdd(&arrivals[counted_chunks(max_parts)], 1u) == nchunks - 1u;
+        if (last) __threadfence();
     }
+    __syncthreads();
+    if (!last) return;
+    scan_chunk_bases(chunk_rows, nchunks, TPD_INBOUNDS(ctl, 19, pass, 8) ? hist[pass][tid] : 0u, wsum, tid);
     if (tid == 0) arrivals[counted_chunks(max_parts)] = 0;
 }
 
@@ -858,9 +913,14 @@ void launch_counted_passes(KeyT* kin, uint32_t* vin, KeyT* kout, uint32_t* vout,
     for (uint32_t p = p0; p < p1; ++p) {
         const uint32_t shift = p * kRadixBits;
         const uint32_t bits = std::min(kRadixBits, plan.key_bits - shift);
-        launch_dependent(partition_count_kernel<16, KeyT>, dim3(max_parts), dim3(256), 0, s, kin, capacity, p, shift,
-                         bits, static_cast<const uint32_t(*)[256]>(hist), plan.fixed_count, max_parts, work, ctl,
-                         abort);
+        if (p == p0 && plan.precounted)
+            launch_dependent(chunk_scan_kernel, dim3(uint32_t(counted_chunks(max_parts))), dim3(256), 0, s, capacity,
+                             p, static_cast<const uint32_t(*)[256]>(hist), plan.fixed_count, max_parts, work, ctl,
+                             abort);
+        else
+            launch_dependent(partition_count_kernel<16, KeyT>, dim3(max_parts), dim3(256), 0, s, kin, capacity, p,
+                             shift, bits, static_cast<const uint32_t(*)[256]>(hist), plan.fixed_count, max_parts,
+                             work, ctl, abort);
         launch_scatter_bits<kItems, kThreads, kMinBlocks, KeyT>(kin, vin, kout, vout, capacity, shift, bits, plan,
                                                                 max_parts, work, ctl,
                                                                 p + 1 == p1 ? plan.ranges : nullptr, abort, s);

@@ -63,6 +63,10 @@ struct PreprocessArgs {
     // visible items will emit, tile ids below 2^tile_bits) go to ctl->sort_hist[0..]
     uint32_t tile_bits;
     FrameCtl* ctl;
+    // words set to zero after the kernel's dependency wait (nullptr: none):
+    // the key sort's precounted rows, for keygen's counts
+    uint32_t* zero_words;
+    uint64_t zero_count;
 };
 
 constexpr uint32_t kMaxViews = 256;
@@ -104,10 +108,13 @@ constexpr uint32_t kKeygenPart = 512;
 // items: where the depth sort leaves the order with no pass skipped;
 // items_other: the other buffer, which holds it when ctl->depth_skips is odd.
 // desc: look-back descriptors (tag ctl->tag * 32 + kTagScan), never cleared.
+// count_rows (or nullptr): the key sort's first counted pass's partition
+// rows, zero on entry (PreprocessArgs.zero_words): each written key adds one
+// to count_rows[256 * (slot / 4096) + (tile & 255)] (SortPlan.precounted).
 void launch_keygen_scan(const Splat* splats, const uint32_t* items, const uint32_t* items_other, uint32_t n_items,
                         uint32_t n, const ViewConst* views, uint32_t* offsets, uint32_t* tiles, uint32_t* vals,
-                        uint32_t capacity, uint32_t* ranges, uint32_t n_tiles, uint64_t* desc, FrameCtl* ctl,
-                        uint32_t spin_limit, uint32_t never_publish, int num_sms, cudaStream_t s);
+                        uint32_t capacity, uint32_t* ranges, uint32_t n_tiles, uint64_t* desc, uint32_t* count_rows,
+                        FrameCtl* ctl, uint32_t spin_limit, uint32_t never_publish, int num_sms, cudaStream_t s);
 
 // keys[i] = tiles[i] << 32 | bits(viewZ of splat vals[i] in the tile's view),
 // i < min(ctl->total_keys, capacity): the 64-bit (tile | depth) keys of a
@@ -151,6 +158,12 @@ struct SortPlan {
     // area of sort_counted_work_words(capacity) u32, zero at rest (every
     // launch leaves it so)
     uint32_t* counted_work = nullptr;
+    // counted passes: the first pass's partition rows (the first
+    // 256 x ceil(capacity / 4096) words of counted_work) already hold every
+    // 4096-key partition's digit counts, added by the kernel that wrote the
+    // keys onto rows that were zero (launch_keygen_scan with count_rows); the
+    // pass only scans them
+    bool precounted = false;
 };
 size_t sort_counted_work_words(uint32_t capacity);
 bool launch_sort(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt, uint32_t capacity,
