@@ -547,7 +547,8 @@ def run_ours(args):
         t = json.loads(tfile.read_text())
         per_key = t.get("counted" if counted else "onesweep")
         traffic = int(per_key * K) if per_key else None
-    pass_kernel = ("partition_count_kernel + scatter_kernel (one counted 8-bit tile-id radix pass of the key sort)"
+    pass_kernel = ("partition_count_kernel (chunk_scan_kernel in the first pass) + scatter_kernel "
+                   "(one counted 8-bit tile-id radix pass of the key sort)"
                    if counted else "onesweep_kernel (one 8-bit tile-id radix pass of the key sort)")
     general = general_sort(eng, K, key_bits, stream, args.steps) if not args.no_general_sort else None
     eng.close()
@@ -616,7 +617,11 @@ def run_ours(args):
                      "moved_GBps": round(K * 16 / (pass_ms / 1000.0) / 1e9, 1),
                      "moved_frac": round(K * 16 / (pass_ms / 1000.0) / 1e9 / hbm, 4),
                      "moved_note": "the pass itself reads and writes 32-bit tile ids and 32-bit values "
-                                   "(16 B per key); the depth half of the keys is ordered by the depth presort"},
+                                   "(16 B per key); the depth half of the keys is ordered by the depth presort",
+                     "time_note": "avg_launch_ms = the key-sort stage / its passes; with counted passes the first "
+                                  "pass's per-partition digit counts are added by keygen_scan_kernel as it writes "
+                                  "the keys (their cost is in the keygen stage, about 0.005 ms at 1080p), and that "
+                                  "pass's counting launch only scans them"},
         "frame_sort": {"keys": K, "key_bits": key_bits, "tile_passes": passes,
                        "depth_sort_ms": round(stage_avg["depth_sort"], 4), "key_sort_ms": round(stage_avg["key_sort"], 4),
                        "formula_GBps": round(sort_formula / ((stage_avg["depth_sort"] + stage_avg["key_sort"]) / 1000) / 1e9, 1),
