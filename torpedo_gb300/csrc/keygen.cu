@@ -1,8 +1,11 @@
-// keygen.cu — kernel (b, second half): key duplication.
+// keygen.cu — kernel (b): the tile-count scan and key duplication, as one
+// kernel over the Gaussians in depth order.
 //
-// Reference: keygen.slang:23-53 (one thread per Gaussian looping over its tile
+// Reference: prefix.slang:40-158 (the scan of the per-Gaussian tile counts)
+// and keygen.slang:23-53 (one thread per Gaussian looping over its tile
 // rect). It also presets the tile ranges (fillBuffer, GaussianEngine.cpp:843-848)
-// that the key sort's last pass fills in (range.slang:18-35, in sort.cu).
+// that the key sort's last pass fills in (range.slang:18-35, in sort.cu), and
+// counts the key sort's first-pass digits per 4096-key partition.
 //
 // GB300 form of keygen: Gaussians are visited in depth order (a prior sort of
 // the (view | depth) keys), so the emitted keys only need a stable sort on
