@@ -14,6 +14,7 @@ raise TpdError like the reference's exceptions.
 from __future__ import annotations
 
 import ctypes as C
+from collections import deque
 from dataclasses import dataclass
 
 import numpy as np
@@ -180,6 +181,7 @@ class GaussianEngine:
         self._h = h
         self.device = device
         self._views: list[Camera] = []
+        self._render_dst: deque = deque()  # destinations of outstanding renders, kept alive until waited for
         self.n = 0
         self.transform_host = TransformHost(self)
 
@@ -217,8 +219,11 @@ class GaussianEngine:
 
     def compile_params(self, means, log_scales, quats, opacity_logits, sh) -> None:
         """Raw parameters as contiguous float32 CUDA tensors on this engine's device."""
+        import torch
+
         for t in (means, log_scales, quats, opacity_logits, sh):
-            assert t.is_cuda and t.dtype.is_floating_point and t.is_contiguous()
+            if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+                raise ValueError("parameters must be contiguous float32 CUDA tensors")
         n = means.shape[0]
         _check(L.load().tpd_compile_params_device(self._h, means.data_ptr(), log_scales.data_ptr(), quats.data_ptr(),
                                                   opacity_logits.data_ptr(), sh.data_ptr(), n), self._h)
@@ -282,7 +287,11 @@ class GaussianEngine:
 
     def read_image_device(self, out) -> None:
         """Copies the packed RGB float image(s) into a contiguous float32 CUDA tensor of pixels*3 elements."""
-        assert out.is_cuda and out.is_contiguous() and out.numel() == self.pixels * 3
+        import torch
+
+        if not (out.is_cuda and out.is_contiguous() and out.dtype == torch.float32
+                and out.numel() == self.pixels * 3):
+            raise ValueError("out must be a contiguous float32 CUDA tensor of pixels * 3 elements")
         _check(L.load().tpd_read_image(self._h, out.data_ptr(), L.TPD_IMAGE_RGB32F, 1), self._h)
 
     def buffer(self, which: int) -> tuple[int, int]:
@@ -329,10 +338,13 @@ class GaussianEngine:
         fmt = L.TPD_IMAGE_RGBA8 if rgba8 else L.TPD_IMAGE_RGB32F
         on_device = 1 if getattr(dst, "is_cuda", False) else 0
         _check(L.load().tpd_render_async(self._h, dst.data_ptr(), fmt, on_device), self._h)
+        self._render_dst.append(dst)  # the copy into dst lands before the matching wait_render returns
 
     def wait_render(self) -> dict:
         st = L.FrameStats()
         _check(L.load().tpd_wait_render(self._h, C.byref(st)), self._h)
+        if self._render_dst:
+            self._render_dst.popleft()
         return st.as_dict()
 
     def step_async(self, dL_dimage, grads, count: int = 1):
