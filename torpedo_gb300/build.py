@@ -31,7 +31,7 @@ SOURCES = {
     "backward.cu": [],
     "engine.cu": [],
     "scan_static.cu": [],
-    "host_util.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "host_util.cpp": ["-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread"],
 }
 
 
@@ -82,7 +82,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     newest = max(o.stat().st_mtime for o in objs)
     if force or not LIB.exists() or LIB.stat().st_mtime < newest:
         tmp = OUT / "libtpdsplat.so.tmp"
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -18,6 +18,7 @@
 #include <random>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/tpdsplat.h"
@@ -260,50 +261,96 @@ int tpd_load_ply(const char* path, void* records, uint32_t* n_out) {
     for (const auto& p : props) if (p.name.rfind("f_rest_", 0) == 0) ++n_rest;
     const int n_feat = std::min(3 + n_rest, 48);
 
-    std::vector<double> vals(props.size());
+    // one record from the properties' values (get(k): property k as a double)
     float* rec = static_cast<float*>(records);
-    for (uint64_t v = 0; v < count; ++v) {
-        if (binary) {
-            for (size_t k = 0; k < props.size(); ++k) {
-                unsigned char buf[8] = {0};
-                if (!f.read(reinterpret_cast<char*>(buf), props[k].size)) return TPD_ERR_IO;
-                double x = 0;
-                switch (props[k].type) {
-                    case 'f': { float t; std::memcpy(&t, buf, 4); x = t; break; }
-                    case 'd': { double t; std::memcpy(&t, buf, 8); x = t; break; }
-                    case 'i': {
-                        if (props[k].size == 4) { int32_t t; std::memcpy(&t, buf, 4); x = t; }
-                        else if (props[k].size == 2) { int16_t t; std::memcpy(&t, buf, 2); x = t; }
-                        else { x = static_cast<int8_t>(buf[0]); }
-                        break;
-                    }
-                    default: {
-                        if (props[k].size == 4) { uint32_t t; std::memcpy(&t, buf, 4); x = t; }
-                        else if (props[k].size == 2) { uint16_t t; std::memcpy(&t, buf, 2); x = t; }
-                        else { x = buf[0]; }
-                    }
-                }
-                vals[k] = x;
-            }
-        } else {
-            for (size_t k = 0; k < props.size(); ++k)
-                if (!(f >> vals[k])) return TPD_ERR_IO;
-        }
-        float* r = rec + v * 60;
+    auto fill = [&](float* r, auto&& get) {
         std::memset(r, 0, 240);
-        r[0] = float(vals[ix]);
-        r[1] = float(vals[iy]);
-        r[2] = float(vals[iz]);
-        r[3] = 1.f / (1.f + std::exp(-float(vals[iop])));
-        float q[4] = {float(vals[ir[1]]), float(vals[ir[2]]), float(vals[ir[3]]), float(vals[ir[0]])};
+        r[0] = float(get(ix));
+        r[1] = float(get(iy));
+        r[2] = float(get(iz));
+        r[3] = 1.f / (1.f + std::exp(-float(get(iop))));
+        float q[4] = {float(get(ir[1])), float(get(ir[2])), float(get(ir[3])), float(get(ir[0]))};
         const float inv = 1.0f / std::sqrt(dot2(q, q, 4));
         for (int k = 0; k < 4; ++k) r[4 + k] = q[k] * inv;
-        for (int k = 0; k < 3; ++k) r[8 + k] = std::exp(float(vals[is[k]]));
+        for (int k = 0; k < 3; ++k) r[8 + k] = std::exp(float(get(is[k])));
         r[11] = 1.f;
         // features: f_dc_0..2 and the properties that follow them, in file order
         for (int k = 0; k < n_feat; ++k) {
             const int pi = idc + k;
-            r[12 + k] = pi < int(props.size()) ? float(vals[pi]) : 0.f;
+            r[12 + k] = pi < int(props.size()) ? float(get(pi)) : 0.f;
+        }
+    };
+    if (binary) {
+        // fixed-size vertices: read kBlock of them at a time and decode each
+        // property from its offset in the vertex (little-endian, as the
+        // format says)
+        std::vector<size_t> off(props.size());
+        size_t stride = 0;
+        for (size_t k = 0; k < props.size(); ++k) {
+            off[k] = stride;
+            stride += size_t(props[k].size);
+        }
+        bool all_float = true;  // the usual 3DGS layout: every property a float32
+        for (const auto& p : props) all_float = all_float && p.type == 'f';
+        // vertices [j0, j1) of a block that starts at vertex v0
+        auto decode = [&](const unsigned char* block, uint64_t v0, uint64_t j0, uint64_t j1) {
+            for (uint64_t j = j0; j < j1; ++j) {
+                const unsigned char* vp = block + j * stride;
+                float* r = rec + (v0 + j) * 60;
+                if (all_float) {
+                    fill(r, [&](int k) -> double {
+                        float t;
+                        std::memcpy(&t, vp + 4 * size_t(k), 4);
+                        return t;
+                    });
+                    continue;
+                }
+                fill(r, [&](int k) -> double {
+                    const unsigned char* b = vp + off[k];
+                    switch (props[k].type) {
+                        case 'f': { float t; std::memcpy(&t, b, 4); return t; }
+                        case 'd': { double t; std::memcpy(&t, b, 8); return t; }
+                        case 'i':
+                            if (props[k].size == 4) { int32_t t; std::memcpy(&t, b, 4); return t; }
+                            if (props[k].size == 2) { int16_t t; std::memcpy(&t, b, 2); return t; }
+                            return static_cast<int8_t>(b[0]);
+                        default:
+                            if (props[k].size == 4) { uint32_t t; std::memcpy(&t, b, 4); return t; }
+                            if (props[k].size == 2) { uint16_t t; std::memcpy(&t, b, 2); return t; }
+                            return b[0];
+                    }
+                });
+            }
+        };
+        // blocks of kBlock vertices, each decoded by up to kThreadsMax host
+        // threads (records are independent: the result does not depend on
+        // the split)
+        constexpr uint64_t kBlock = 1u << 17;
+        constexpr unsigned kThreadsMax = 16;
+        const unsigned hw = std::max(1u, std::min(kThreadsMax, std::thread::hardware_concurrency()));
+        std::vector<unsigned char> block;
+        for (uint64_t v0 = 0; v0 < count; v0 += kBlock) {
+            const uint64_t nv = std::min(kBlock, count - v0);
+            block.resize(nv * stride);
+            if (!f.read(reinterpret_cast<char*>(block.data()), std::streamsize(nv * stride))) return TPD_ERR_IO;
+            const unsigned nt = unsigned(std::min<uint64_t>(hw, (nv + 4095) / 4096));
+            if (nt <= 1) {
+                decode(block.data(), v0, 0, nv);
+                continue;
+            }
+            std::vector<std::thread> pool;
+            pool.reserve(nt - 1);
+            for (unsigned t = 1; t < nt; ++t)
+                pool.emplace_back(decode, block.data(), v0, nv * t / nt, nv * (t + 1) / nt);
+            decode(block.data(), v0, 0, nv / nt);
+            for (auto& th : pool) th.join();
+        }
+    } else {
+        std::vector<double> vals(props.size());
+        for (uint64_t v = 0; v < count; ++v) {
+            for (size_t k = 0; k < props.size(); ++k)
+                if (!(f >> vals[k])) return TPD_ERR_IO;
+            fill(rec + v * 60, [&](int k) { return vals[k]; });
         }
     }
     return TPD_OK;

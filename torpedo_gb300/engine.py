@@ -122,7 +122,7 @@ def load_ply(path: str) -> np.ndarray:
     lib = L.load()
     n = C.c_uint32(0)
     _check(lib.tpd_load_ply(str(path).encode(), None, C.byref(n)))
-    rec = np.zeros((n.value, 60), np.float32)
+    rec = np.empty((n.value, 60), np.float32)  # every record is written in full
     _check(lib.tpd_load_ply(str(path).encode(), rec.ctypes.data, C.byref(n)))
     return rec
 
