@@ -1,5 +1,5 @@
-"""View sharding of the batched backward across two ranks (gloo, CPU): each
-rank differentiates its share of the views with the FP64 oracle, one
+"""View sharding of the batched backward across two and three ranks (gloo,
+CPU): each rank differentiates its share of the views with the FP64 oracle, one
 all-reduce sums the per-Gaussian gradients, and the result equals the
 gradient of the whole batch computed in one process."""
 import os
@@ -74,11 +74,13 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def test_sharded_backward_allreduce_equals_whole_batch(tmp_path):
+@pytest.mark.parametrize("world", [2, 3])
+def test_sharded_backward_allreduce_equals_whole_batch(tmp_path, world):
+    """World size 3 splits the five views of uneven sizes unevenly (a rank
+    with one view beside ranks with two)."""
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
 
-    world = 2
     mp.spawn(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
     sc, cams, params = _setup()
     whole = [np.zeros_like(p) for p in params]
